@@ -1,0 +1,196 @@
+"""Seeded synthetic least-squares problems with the shapes of the AMFLS workloads.
+
+No public dataset is involved: every matrix is drawn from a numpy
+``Generator`` seeded by the caller, so a (family, sizes, seed) triple names a
+problem exactly.  CSR matrices are returned as numpy arrays
+(``row_offsets`` int64, ``column_indices`` int64 sorted within each row,
+``values`` float64), the layout ``torch.sparse_csr_tensor`` and the reference's
+``SparseCsrOperator`` both accept (sparse_csr_operator.hpp:13-21).
+
+Families
+--------
+``scaled_uniform_csr``  fixed nonzeros per row at distinct uniform columns,
+    N(0,1) values with column j scaled by 10^(-decades*j/n); b = A x + noise.
+    At m=20000, n=5000, 10 per row, 6 decades, noise 1e-8 this is the
+    CPU-runnable 20000x5000 CSR workload.
+``power_law_csr``  row lengths L = min(L_max, ceil(x_m U^-2)), U ~ U(0,1]
+    (tail exponent 1.5); with x_m = 0.04688 the mean is 20 and nnz is about
+    20 m.  At m=2,000,000, n=500,000, 8 decades, noise 1e-6 this is the
+    2Mx500k CSR workload.
+``banded_random_csr``  a band of ``band`` columns centred on floor(i n / m)
+    plus ``off_band`` distinct uniform columns, 10^(-decades*j/n) scaling
+    (the 4Mx1M learned-width family).
+``scaled_dense``  G diag(d) with G i.i.d. N(0,1), d geometric from 1 to
+    10^-decades, b ~ N(0,1) (the 100000x2000 dense workload).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+@dataclass
+class CsrProblem:
+    rows: int
+    cols: int
+    row_offsets: np.ndarray
+    column_indices: np.ndarray
+    values: np.ndarray
+    b: np.ndarray
+    x_true: np.ndarray | None = None
+
+    @property
+    def nnz(self) -> int:
+        return int(self.values.shape[0])
+
+    def to_dense(self) -> np.ndarray:
+        a = np.zeros((self.rows, self.cols))
+        row_ids = np.repeat(np.arange(self.rows), np.diff(self.row_offsets))
+        a[row_ids, self.column_indices] = self.values
+        return a
+
+    def matvec(self, x: np.ndarray) -> np.ndarray:
+        row_ids = np.repeat(np.arange(self.rows), np.diff(self.row_offsets))
+        return np.bincount(row_ids, weights=self.values * x[self.column_indices],
+                           minlength=self.rows)
+
+
+@dataclass
+class DenseProblem:
+    matrix: np.ndarray  # shape (rows, cols); contiguity tells the layout
+    b: np.ndarray
+
+    @property
+    def rows(self) -> int:
+        return int(self.matrix.shape[0])
+
+    @property
+    def cols(self) -> int:
+        return int(self.matrix.shape[1])
+
+
+def _distinct_columns(rng: np.random.Generator, lengths: np.ndarray, n: int) -> np.ndarray:
+    """Uniform column indices, distinct within each row, sorted within each row."""
+    lengths = np.minimum(lengths.astype(np.int64), n)
+    total = int(lengths.sum())
+    row_ids = np.repeat(np.arange(lengths.shape[0], dtype=np.int64), lengths)
+    cols = rng.integers(0, n, size=total, dtype=np.int64)
+    while True:
+        key = row_ids * n + cols
+        order = np.argsort(key, kind="stable")
+        key_sorted = key[order]
+        dup = np.zeros(total, dtype=bool)
+        dup[1:] = key_sorted[1:] == key_sorted[:-1]
+        if not dup.any():
+            return key_sorted - row_ids * n  # rows stay in order; columns sorted
+        redo = order[dup]
+        cols[redo] = rng.integers(0, n, size=redo.shape[0], dtype=np.int64)
+
+
+def _finish_csr(rng, m, n, lengths, cols, decades, noise):
+    offsets = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(lengths, out=offsets[1:])
+    values = rng.standard_normal(cols.shape[0])
+    values *= 10.0 ** (-decades * cols.astype(np.float64) / n)
+    prob = CsrProblem(m, n, offsets, cols, values, np.zeros(m))
+    x_true = rng.standard_normal(n)
+    b = prob.matvec(x_true)
+    if noise:
+        b = b + noise * rng.standard_normal(m)
+    prob.b = b
+    prob.x_true = x_true
+    return prob
+
+
+def scaled_uniform_csr(m: int, n: int, per_row: int = 10, decades: float = 6.0,
+                       noise: float = 1e-8, seed: int = 0) -> CsrProblem:
+    rng = np.random.default_rng(seed)
+    lengths = np.full(m, min(per_row, n), dtype=np.int64)
+    cols = _distinct_columns(rng, lengths, n)
+    return _finish_csr(rng, m, n, lengths, cols, decades, noise)
+
+
+def power_law_csr(m: int, n: int, x_m: float = 0.04688, max_row: int = 2000,
+                  decades: float = 8.0, noise: float = 1e-6, seed: int = 0) -> CsrProblem:
+    rng = np.random.default_rng(seed)
+    u = 1.0 - rng.random(m)  # (0, 1]
+    lengths = np.minimum(max_row, np.ceil(x_m * u ** -2.0)).astype(np.int64)
+    lengths = np.minimum(np.maximum(lengths, 1), n)
+    cols = _distinct_columns(rng, lengths, n)
+    return _finish_csr(rng, m, n, lengths, cols, decades, noise)
+
+
+def banded_random_csr(m: int, n: int, band: int = 8, off_band: int = 8,
+                      decades: float = 9.0, noise: float = 0.0, seed: int = 0) -> CsrProblem:
+    rng = np.random.default_rng(seed)
+    centre = (np.arange(m, dtype=np.int64) * n) // m
+    start = np.clip(centre - band // 2, 0, max(0, n - band))
+    band_cols = start[:, None] + np.arange(band, dtype=np.int64)[None, :]
+    extra = _distinct_columns(rng, np.full(m, off_band + band, dtype=np.int64), n)
+    extra = extra.reshape(m, off_band + band)
+    merged = []
+    for i in range(0, m, 65536):  # keep the per-chunk work bounded
+        b_c = band_cols[i:i + 65536]
+        e_c = extra[i:i + 65536]
+        keep = ~(e_c[:, :, None] == b_c[:, None, :]).any(axis=2)
+        # take the first off_band extra columns that miss the band
+        rank = np.cumsum(keep, axis=1)
+        sel = keep & (rank <= off_band)
+        rows_sel = np.where(sel.sum(axis=1) == off_band)[0]
+        if rows_sel.shape[0] != b_c.shape[0]:
+            raise RuntimeError("band overlap exhausted the off-band candidates")
+        chosen = e_c[sel].reshape(-1, off_band)
+        merged.append(np.sort(np.concatenate([b_c, chosen], axis=1), axis=1))
+    cols = np.concatenate(merged, axis=0).reshape(-1)
+    lengths = np.full(m, band + off_band, dtype=np.int64)
+    return _finish_csr(rng, m, n, lengths, cols, decades, noise)
+
+
+def scaled_dense(m: int, n: int, decades: float = 6.0, seed: int = 0,
+                 column_major: bool = True) -> DenseProblem:
+    rng = np.random.default_rng(seed)
+    d = 10.0 ** (-decades * np.arange(n) / max(1, n - 1))
+    if column_major:
+        g = np.asfortranarray(rng.standard_normal((n, m)).T)
+    else:
+        g = rng.standard_normal((m, n))
+    g *= d[None, :]
+    b = rng.standard_normal(m)
+    return DenseProblem(g, b)
+
+
+# The named workloads (full sizes).  Each entry gives the generator, its
+# keyword arguments and the solver options.
+WORKLOADS = {
+    "csr_20000x5000": dict(
+        family="scaled_uniform_csr",
+        kwargs=dict(m=20000, n=5000, per_row=10, decades=6.0, noise=1e-8),
+        options=dict(regularization=0.0, tolerance=1e-8)),
+    "dense_100000x2000": dict(
+        family="scaled_dense",
+        kwargs=dict(m=100000, n=2000, decades=6.0),
+        options=dict(regularization=1e-6, tolerance=1e-10)),
+    "csr_2000000x500000": dict(
+        family="power_law_csr",
+        kwargs=dict(m=2_000_000, n=500_000, decades=8.0, noise=1e-6),
+        options=dict(regularization=1e-4, tolerance=1e-10)),
+    "csr_4000000x1000000": dict(
+        family="banded_random_csr",
+        kwargs=dict(m=4_000_000, n=1_000_000, decades=9.0),
+        options=dict(regularization=0.0, tolerance=1e-10, maximum_auxiliary_width=64)),
+}
+
+FAMILIES = {
+    "scaled_uniform_csr": scaled_uniform_csr,
+    "power_law_csr": power_law_csr,
+    "banded_random_csr": banded_random_csr,
+    "scaled_dense": scaled_dense,
+}
+
+
+def make(name: str, seed: int = 0, **overrides):
+    spec = WORKLOADS[name]
+    kwargs = dict(spec["kwargs"])
+    kwargs.update(overrides)
+    return FAMILIES[spec["family"]](seed=seed, **kwargs), dict(spec["options"])

@@ -1,0 +1,51 @@
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLDEN = Path(__file__).resolve().parent / "golden"
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def load_golden(name):
+    """Fixture arrays plus the problem object they describe."""
+    from amfls_solver_gb300 import problems
+
+    data = dict(np.load(GOLDEN / f"{name}.npz"))
+    kind = int(data["kind"])
+    if kind == 0:
+        prob = problems.CsrProblem(int(data["rows"]), int(data["cols"]), data["row_offsets"],
+                                   data["column_indices"], data["values"], data["b"])
+    else:
+        mat = data["matrix"]
+        mat = np.ascontiguousarray(mat) if kind == 1 else np.asfortranarray(mat)
+        prob = problems.DenseProblem(mat, data["b"])
+    return data, prob
+
+
+def golden_options(data):
+    o, i = data["options"], data["int_options"]
+    opts = dict(regularization=float(o[0]), tolerance=float(o[1]),
+                failure_probability=float(o[2]), seed=int(i[4]), stream=int(i[5]))
+    if int(i[7]) == 1:
+        opts.update(algorithm="fixed_rbgk", auxiliary_width=int(i[6]),
+                    maximum_depth=int(i[1]), maximum_basis_size=int(i[3]))
+    else:
+        opts.update(maximum_epochs=int(i[0]), maximum_depth=int(i[1]),
+                    maximum_auxiliary_width=int(i[2]), maximum_basis_size=int(i[3]))
+    return opts
+
+
+SOLVE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("solve_*.npz"))
+
+
+@pytest.fixture(scope="session")
+def golden():
+    return load_golden

@@ -1,0 +1,160 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run (where the reference sources exist):
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Each fixture holds the exact inputs and the reference's outputs, produced by
+oracle/_ref/libamfls_ref.so (the reference's AMFLS sources compiled where they
+lie, see oracle/Makefile).  Fixtures are small (sizes the oracle and a GPU
+finish in well under a second) and self-contained, so tests on a machine
+without the reference read them as plain data.
+
+Only deterministic runs are stored: CSR operators never widen under the
+reference's default cost model, and fixed-width RBGK has no width controller.
+AMFLS widening on dense operators depends on measured seconds and is not
+reproducible across machines, so dense AMFLS fixtures use cases whose
+outcome does not depend on timing (basis-limited ridge, maximum_epochs=0 with
+auxiliary width 0, or a depth cap of one level).
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from amfls_solver_gb300 import problems  # noqa: E402
+from oracle import ref  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def save(name, **arrays):
+    np.savez_compressed(OUT / f"{name}.npz", **arrays)
+    print("wrote", name)
+
+
+def csr_arrays(p):
+    return dict(kind=np.int64(0), rows=np.int64(p.rows), cols=np.int64(p.cols),
+                row_offsets=p.row_offsets, column_indices=p.column_indices,
+                values=p.values, b=p.b)
+
+
+def dense_arrays(p):
+    kind = 1 if p.matrix.flags.c_contiguous else 2
+    return dict(kind=np.int64(kind), rows=np.int64(p.rows), cols=np.int64(p.cols),
+                matrix=np.array(p.matrix), b=p.b)
+
+
+def solve_fixture(name, p, arrays, **opts):
+    r = ref.solve(p, **opts)
+    options = np.array([opts.get("regularization", 0.0), opts.get("tolerance", 1e-8),
+                        opts.get("failure_probability", 1e-6)])
+    ints = np.array([opts.get("maximum_epochs", 0), opts.get("maximum_depth", 0),
+                     opts.get("maximum_auxiliary_width", 0),
+                     opts.get("maximum_basis_size", 0), opts.get("seed", 0),
+                     opts.get("stream", 0), opts.get("auxiliary_width", 4),
+                     1 if opts.get("algorithm", "amfls") == "fixed_rbgk" else 0],
+                    dtype=np.int64)
+    save(name, **arrays, options=options, int_options=ints, solution=r["solution"],
+         metrics=r["metrics"], counters=r["counters"], trace_float=r["trace_float"],
+         trace_int=r["trace_int"], status=np.int64(r["status"]),
+         stop_reason=np.int64(r["stop_reason"]))
+    c = r["counters"]
+    print(f"   status {r['status']}/{r['stop_reason']} depth {c[9]} aux {c[10]} "
+          f"basis {c[11]} evals {len(r['trace_int'])} disp {c[35]}")
+
+
+def main():
+    # ---- kernels: CSR products, validation model, Gaussian, norm intervals
+    p = problems.scaled_uniform_csr(300, 120, per_row=7, decades=3.0, seed=11)
+    rng = np.random.default_rng(5)
+    x = np.asfortranarray(rng.standard_normal((120, 3)))
+    y = np.asfortranarray(rng.standard_normal((300, 3)))
+    model, steps = ref.validation_model(p)
+    save("csr_products", **csr_arrays(p), x=x, y=y,
+         ax1=ref.apply(p, x[:, 0]), aty1=ref.apply(p, y[:, 0], transpose=True),
+         ax3=ref.apply(p, x), aty3=ref.apply(p, y, transpose=True),
+         model=model, steps=steps)
+    # ragged rows: empty rows, one heavy row, an empty column
+    m, n = 64, 40
+    lengths = rng.integers(0, 6, size=m)
+    lengths[3] = 0
+    lengths[10] = 39
+    cols = problems._distinct_columns(rng, lengths, n - 1)  # last column empty
+    off = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(lengths, out=off[1:])
+    q = problems.CsrProblem(m, n, off, cols, rng.standard_normal(cols.shape[0]), np.zeros(m))
+    xr = rng.standard_normal(n)
+    yr = rng.standard_normal(m)
+    model, steps = ref.validation_model(q)
+    save("csr_ragged", **csr_arrays(q), x=xr, y=yr, ax1=ref.apply(q, xr),
+         aty1=ref.apply(q, yr, transpose=True), model=model, steps=steps)
+
+    for tag, dp in (("rm", problems.scaled_dense(50, 17, decades=4.0, seed=3, column_major=False)),
+                    ("cm", problems.scaled_dense(50, 17, decades=4.0, seed=3, column_major=True))):
+        model, steps = ref.validation_model(dp)
+        save(f"dense_model_{tag}", **dense_arrays(dp), model=model, steps=steps)
+
+    gauss = []
+    params = [(37, 5, 12345, 7, 3), (16, 2, 0, 0, 0), (9, 3, 2**64 - 1, 2**63 + 5, 17)]
+    for rows, cols_, seed, stream, first in params:
+        gauss.append(ref.gaussian_matrix(rows, cols_, seed, stream, first))
+    save("gaussian", params=np.array(params, dtype=np.uint64),
+         g0=gauss[0], g1=gauss[1], g2=gauss[2])
+
+    vecs = [rng.standard_normal(1000),
+            np.concatenate([rng.standard_normal(10) * 1e-310, [0.0, 5e-324]]),
+            np.zeros(17), rng.standard_normal(33) * 1e300, np.array([3.0, -4.0])]
+    bounds = np.array([ref.norm_interval(v) for v in vecs])
+    save("norm_interval", **{f"v{i}": v for i, v in enumerate(vecs)}, bounds=bounds)
+
+    # ---- end-to-end solves
+    c1 = problems.scaled_uniform_csr(2000, 500, seed=1)
+    solve_fixture("solve_csr_ls", c1, csr_arrays(c1), regularization=0.0, tolerance=1e-8, seed=7)
+    solve_fixture("solve_csr_ridge", c1, csr_arrays(c1), regularization=1e-4, tolerance=1e-10,
+                  seed=7)
+    c2 = problems.power_law_csr(3000, 800, decades=4.0, noise=1e-6, seed=4)
+    solve_fixture("solve_powerlaw_ridge", c2, csr_arrays(c2), regularization=1e-4,
+                  tolerance=1e-10)
+    c3 = problems.scaled_uniform_csr(600, 1500, per_row=12, decades=3.0, noise=1e-3, seed=9)
+    solve_fixture("solve_csr_wide", c3, csr_arrays(c3), regularization=0.0, tolerance=1e-8)
+    # inconsistent, tight tolerance: exercises the extended-precision refinement
+    c4 = problems.scaled_uniform_csr(1500, 200, per_row=6, decades=2.0, noise=1.0, seed=21)
+    solve_fixture("solve_csr_inconsistent", c4, csr_arrays(c4), regularization=0.0,
+                  tolerance=1e-13)
+    solve_fixture("solve_csr_depth_cap", c1, csr_arrays(c1), regularization=0.0, tolerance=1e-8,
+                  maximum_depth=40)
+    solve_fixture("solve_csr_basis_cap", c1, csr_arrays(c1), regularization=1e-4,
+                  tolerance=1e-12, maximum_basis_size=30)
+    z = problems.scaled_uniform_csr(200, 50, seed=2)
+    z.b = np.zeros(200)
+    solve_fixture("solve_csr_zero_rhs", z, csr_arrays(z), regularization=0.0, tolerance=1e-8)
+    # rank deficient: every column appears twice with proportional values
+    half = problems.scaled_uniform_csr(400, 60, per_row=5, decades=1.0, noise=0.0, seed=13)
+    dup_cols = np.stack([half.column_indices, half.column_indices + 60], axis=1).reshape(-1)
+    dup_vals = np.stack([half.values, 2.0 * half.values], axis=1).reshape(-1)
+    rd = problems.CsrProblem(400, 120, half.row_offsets * 2, dup_cols, dup_vals,
+                             half.b.copy())
+    solve_fixture("solve_csr_rank_deficient", rd, csr_arrays(rd), regularization=0.0,
+                  tolerance=1e-8)
+
+    d1 = problems.scaled_dense(600, 80, decades=6.0, seed=2, column_major=False)
+    solve_fixture("solve_dense_rm_ridge_basis", d1, dense_arrays(d1), regularization=1e-6,
+                  tolerance=1e-12, maximum_epochs=1, maximum_auxiliary_width=1)
+    d2 = problems.scaled_dense(600, 80, decades=3.0, seed=5, column_major=True)
+    solve_fixture("solve_dense_cm_depth1", d2, dense_arrays(d2), regularization=0.0,
+                  tolerance=1e-10, maximum_depth=1)
+    solve_fixture("solve_fixed_rbgk_dense", d2, dense_arrays(d2), algorithm="fixed_rbgk",
+                  regularization=0.0, tolerance=1e-10, auxiliary_width=3, maximum_depth=40,
+                  seed=11, stream=2)
+    solve_fixture("solve_fixed_rbgk_csr_ridge", c1, csr_arrays(c1), algorithm="fixed_rbgk",
+                  regularization=1e-4, tolerance=1e-10, auxiliary_width=7, maximum_depth=60,
+                  seed=3)
+
+
+if __name__ == "__main__":
+    main()
