@@ -1,0 +1,25 @@
+"""GB300-native AMFLS: adaptive-width block Golub-Kahan least squares on sm_103a.
+
+Drop-in for the reference's python/amfls package on CUDA tensors:
+``run_amfls``, ``run_fixed_rbgk``, ``SolveResult``, ``load_library`` and
+``torch.ops.amfls.run_amfls`` / ``run_fixed_rbgk`` with the reference's schema.
+The compute path is the native library libamfls_gb300.so (C ABI in
+include/amfls_gpu.h); importing this package never falls back to the CPU.
+"""
+from .binding import (
+    DeviceOperator,
+    SolveResult,
+    load_library,
+    register_torch_ops,
+    run_amfls,
+    run_fixed_rbgk,
+)
+
+__all__ = [
+    "DeviceOperator",
+    "SolveResult",
+    "load_library",
+    "register_torch_ops",
+    "run_amfls",
+    "run_fixed_rbgk",
+]

@@ -1,0 +1,417 @@
+"""PyTorch binding of the GB300 AMFLS solver (CUDA tensors).
+
+Mirrors the reference's python/amfls/binding.py (SolveResult :9-90,
+load_library :92-97, _decode :159-255, run_amfls :259-290) and its torch op
+``torch.ops.amfls.run_amfls`` (bindings/torch/torch_binding.cpp:510-516,
+same schema string and 8-tuple), registered here for the CUDA and
+SparseCsrCUDA dispatch keys.  When the reference's CPU library is loaded in
+the same process the op already exists; only the CUDA kernels are added, so
+one op dispatches to the reference on CPU tensors and to this library on
+CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import _native
+
+TRACE_CAPACITY = 16384
+
+RUN_AMFLS_SCHEMA = (
+    "run_amfls(Tensor matrix, Tensor b, float regularization, float tolerance, "
+    "float failure_probability, int maximum_epochs=0, int maximum_depth=0, "
+    "int maximum_auxiliary_width=0, int maximum_basis_size=0, "
+    "int seed=0, int stream=0) -> "
+    "(Tensor, Tensor, Tensor, Tensor, Tensor, Tensor, int, int)")
+RUN_FIXED_RBGK_SCHEMA = (
+    "run_fixed_rbgk(Tensor matrix, Tensor b, float regularization, float tolerance, "
+    "float failure_probability, int auxiliary_width, int maximum_depth, "
+    "int maximum_basis_size, int seed, int stream) -> "
+    "(Tensor, Tensor, Tensor, Tensor, Tensor, Tensor, int, int)")
+
+
+@dataclass(frozen=True)
+class SolveResult:
+    solution: torch.Tensor
+    objective: float
+    residual_norm: float
+    augmented_residual_norm: float
+    normal_residual_norm: float
+    solution_norm: float
+    solution_energy_norm: float
+    operator_norm_lower_bound: float
+    augmented_operator_norm_lower_bound: float
+    compatible_backward_error_upper_bound: float
+    least_squares_backward_error_upper_bound: float
+    backward_error_upper_bound: float
+    relative_normal_residual_upper_bound: float
+    energy_error_upper_bound: float
+    relative_energy_error_upper_bound: float
+    objective_gap_upper_bound: float
+    ridge_base_energy_error_upper_bound: float | None
+    ridge_corrected_energy_error_upper_bound: float | None
+    ridge_correction_gamma: float | None
+    ridge_correction_z_h_z: float | None
+    ridge_correction_two_abs_z_t_q: float | None
+    ridge_correction_q_norm_squared: float | None
+    a_columns: int
+    at_columns: int
+    a_block_calls: int
+    at_block_calls: int
+    search_a_columns: int
+    search_at_columns: int
+    validation_a_columns: int
+    validation_at_columns: int
+    iterations: int
+    depth: int
+    auxiliary_width: int
+    basis_rank: int
+    sketch_a_columns: int
+    sketch_at_columns: int
+    sketch_a_block_calls: int
+    sketch_at_block_calls: int
+    iterative_a_columns: int
+    iterative_at_columns: int
+    iterative_a_block_calls: int
+    iterative_at_block_calls: int
+    gaussian_random_columns: int
+    gaussian_random_values: int
+    search_a_block_calls: int
+    search_at_block_calls: int
+    validation_a_block_calls: int
+    validation_at_block_calls: int
+    base_validation_a_columns: int
+    base_validation_at_columns: int
+    base_validation_a_block_calls: int
+    base_validation_at_block_calls: int
+    ridge_correction_a_columns: int
+    ridge_correction_at_columns: int
+    ridge_correction_a_block_calls: int
+    ridge_correction_at_block_calls: int
+    gaussian_random_block_requests: int
+    ridge_correction_disposition: int
+    total_seconds: float
+    a_seconds: float
+    at_seconds: float
+    orthogonalization_seconds: float
+    projected_solve_seconds: float
+    validation_seconds: float
+    other_seconds: float
+    base_validation_seconds: float
+    ridge_correction_validation_seconds: float
+    trace: torch.Tensor
+    trace_float: torch.Tensor
+    trace_int: torch.Tensor
+    status: int
+    stop_reason: int
+
+    @property
+    def success(self) -> bool:
+        return self.status == 0
+
+    @property
+    def search_vector_work(self) -> int:
+        return self.search_a_columns + self.search_at_columns
+
+
+_METRIC_NAMES = [
+    "objective", "residual_norm", "augmented_residual_norm", "normal_residual_norm",
+    "solution_norm", "solution_energy_norm", "operator_norm_lower_bound",
+    "augmented_operator_norm_lower_bound", "compatible_backward_error_upper_bound",
+    "least_squares_backward_error_upper_bound", "backward_error_upper_bound",
+    "relative_normal_residual_upper_bound", "energy_error_upper_bound",
+    "relative_energy_error_upper_bound", "objective_gap_upper_bound",
+    "ridge_base_energy_error_upper_bound", "ridge_corrected_energy_error_upper_bound",
+    "ridge_correction_gamma", "ridge_correction_z_h_z", "ridge_correction_two_abs_z_t_q",
+    "ridge_correction_q_norm_squared"]
+_COUNTER_NAMES = [
+    "a_columns", "at_columns", "a_block_calls", "at_block_calls", "search_a_columns",
+    "search_at_columns", "validation_a_columns", "validation_at_columns", "iterations", "depth",
+    "auxiliary_width", "basis_rank", "sketch_a_columns", "sketch_at_columns",
+    "sketch_a_block_calls", "sketch_at_block_calls", "iterative_a_columns",
+    "iterative_at_columns", "iterative_a_block_calls", "iterative_at_block_calls",
+    "gaussian_random_columns", "gaussian_random_values", "search_a_block_calls",
+    "search_at_block_calls", "validation_a_block_calls", "validation_at_block_calls",
+    "base_validation_a_columns", "base_validation_at_columns", "base_validation_a_block_calls",
+    "base_validation_at_block_calls", "ridge_correction_a_columns", "ridge_correction_at_columns",
+    "ridge_correction_a_block_calls", "ridge_correction_at_block_calls",
+    "gaussian_random_block_requests", "ridge_correction_disposition"]
+_TIMING_NAMES = [
+    "total_seconds", "a_seconds", "at_seconds", "orthogonalization_seconds",
+    "projected_solve_seconds", "validation_seconds", "other_seconds", "base_validation_seconds",
+    "ridge_correction_validation_seconds"]
+
+
+# ------------------------------------------------------------ operators ----
+
+def _stream_handle(device: torch.device | None = None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class DeviceOperator:
+    """A device MatrixOperator (CSR or dense) owned by the native library.
+
+    CSR inputs are copied and validated (like the reference's
+    SparseCsrOperator constructor); dense inputs are referenced in place, so
+    the tensor is kept alive by this object.
+    """
+
+    def __init__(self, matrix: torch.Tensor):
+        lib = _native.load()
+        if matrix.device.type != "cuda":
+            raise ValueError("the GB300 binding supports CUDA tensors only")
+        if matrix.dtype != torch.float64:
+            raise ValueError("matrix must use torch.float64")
+        if matrix.dim() != 2 or matrix.shape[0] <= 0 or matrix.shape[1] <= 0:
+            raise ValueError("matrix must have shape (m,n) with m, n > 0")
+        if matrix.shape[0] > 2**31 - 1 or matrix.shape[1] > 2**31 - 1:
+            raise ValueError("matrix exceeds the LP64 dimension limit")
+        self.rows, self.cols = int(matrix.shape[0]), int(matrix.shape[1])
+        handle = ctypes.c_void_p()
+        stream = _stream_handle(matrix.device)
+        with torch.cuda.device(matrix.device):
+            if matrix.layout == torch.sparse_csr:
+                crow = matrix.crow_indices().to(torch.int64).contiguous()
+                col = matrix.col_indices().to(torch.int64).contiguous()
+                val = matrix.values().contiguous()
+                if crow.numel() != self.rows + 1:
+                    raise ValueError("CSR row offsets must have length rows + 1")
+                if col.numel() != val.numel():
+                    raise ValueError("CSR column indices and values must be equally sized")
+                _native.check(lib.amfls_gpu_csr_operator_create(
+                    self.rows, self.cols, crow.data_ptr(), col.data_ptr(), val.data_ptr(),
+                    val.numel(), stream, ctypes.byref(handle)))
+                self._keep = None
+            elif matrix.layout == torch.strided:
+                dense = matrix.contiguous()
+                _native.check(lib.amfls_gpu_dense_operator_create(
+                    self.rows, self.cols, dense.data_ptr(), 0, stream, ctypes.byref(handle)))
+                self._keep = dense
+            else:
+                raise ValueError("matrix must use dense strided or sparse CSR storage")
+        self.handle = handle
+        self.device = matrix.device
+
+    @classmethod
+    def from_csr_arrays(cls, rows, cols, row_offsets, column_indices, values):
+        """CSR operator from device tensors (int64 offsets/indices, float64 values)."""
+        t = torch.sparse_csr_tensor(row_offsets, column_indices, values, size=(rows, cols))
+        return cls(t)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _native.load().amfls_gpu_operator_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def apply(self, x: torch.Tensor, transpose: bool = False) -> torch.Tensor:
+        """Y = A X (or X = A^T Y) for a column-major block given as (k, s) or (k,)."""
+        lib = _native.load()
+        vec = x.dim() == 1
+        xs = x.reshape(-1, 1) if vec else x
+        s = xs.shape[1]
+        xc = xs.t().contiguous()  # column-major storage of the block
+        out_rows = self.cols if transpose else self.rows
+        yc = torch.empty((s, out_rows), dtype=torch.float64, device=x.device)
+        fn = lib.amfls_gpu_operator_apply_transpose if transpose else lib.amfls_gpu_operator_apply
+        _native.check(fn(self.handle, xc.data_ptr(), s, yc.data_ptr(), _stream_handle(x.device)))
+        y = yc.t()
+        return y.reshape(-1) if vec else y
+
+    def validation_error_model(self):
+        m = _native.ValidationModel()
+        _native.check(_native.load().amfls_gpu_operator_validation_error_model(
+            self.handle, ctypes.byref(m)))
+        return (m.operator_norm_upper_bound, m.operator_norm_lower_bound,
+                m.apply_rounding_steps, m.apply_transpose_rounding_steps)
+
+    def relative_block_product_cost(self, block_cols: int) -> float:
+        return _native.load().amfls_gpu_operator_relative_block_product_cost(
+            self.handle, block_cols)
+
+
+# --------------------------------------------------------------- solves ----
+
+def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options: _native.Options):
+    lib = _native.load()
+    if b.device != op.device:
+        raise ValueError("matrix and b must be on the same CUDA device")
+    b = b.contiguous()
+    x = torch.empty(op.cols, dtype=torch.float64, device=b.device)
+    res = _native.Result()
+    tf = np.zeros((TRACE_CAPACITY, 29))
+    ti = np.zeros((TRACE_CAPACITY, 4), dtype=np.int64)
+    fn = lib.amfls_gpu_solve_amfls if algorithm == "amfls" else lib.amfls_gpu_solve_fixed_rbgk
+    with torch.cuda.device(b.device):
+        _native.check(fn(op.handle, b.data_ptr(), ctypes.byref(options), x.data_ptr(),
+                         ctypes.byref(res), tf.ctypes.data, ti.ctypes.data, TRACE_CAPACITY,
+                         _stream_handle(b.device)))
+    rows = min(res.trace_rows, TRACE_CAPACITY)
+    return (x,
+            torch.tensor(list(res.metrics), dtype=torch.float64),
+            torch.tensor(list(res.counters), dtype=torch.int64),
+            torch.tensor(list(res.timings), dtype=torch.float64),
+            torch.from_numpy(tf[:rows].copy()),
+            torch.from_numpy(ti[:rows].copy()),
+            int(res.status), int(res.stop_reason))
+
+
+def _uint64(v: int) -> int:
+    return int(v) & (2**64 - 1)
+
+
+def _run_amfls_impl(matrix, b, regularization, tolerance, failure_probability,
+                    maximum_epochs=0, maximum_depth=0, maximum_auxiliary_width=0,
+                    maximum_basis_size=0, seed=0, stream=0):
+    _check_inputs(matrix, b)
+    op = DeviceOperator(matrix)
+    o = _native.default_options()
+    o.regularization = float(regularization)
+    o.tolerance = float(tolerance)
+    o.failure_probability = float(failure_probability)
+    o.maximum_epochs = int(maximum_epochs)
+    o.maximum_depth = int(maximum_depth)
+    o.maximum_auxiliary_width = int(maximum_auxiliary_width)
+    o.maximum_basis_size = int(maximum_basis_size)
+    o.seed = _uint64(seed)
+    o.stream = _uint64(stream)
+    return _solve_raw("amfls", op, b, o)
+
+
+def _run_fixed_rbgk_impl(matrix, b, regularization, tolerance, failure_probability,
+                         auxiliary_width, maximum_depth, maximum_basis_size, seed, stream):
+    _check_inputs(matrix, b)
+    op = DeviceOperator(matrix)
+    o = _native.default_options()
+    o.regularization = float(regularization)
+    o.tolerance = float(tolerance)
+    o.failure_probability = float(failure_probability)
+    o.auxiliary_width = int(auxiliary_width)
+    o.maximum_depth = int(maximum_depth)
+    o.maximum_basis_size = int(maximum_basis_size)
+    o.seed = _uint64(seed)
+    o.stream = _uint64(stream)
+    return _solve_raw("fixed_rbgk", op, b, o)
+
+
+_LIBS = []
+
+
+def _op_exists(name: str) -> bool:
+    try:
+        getattr(torch.ops.amfls, name)
+        return True
+    except (AttributeError, RuntimeError):
+        return False
+
+
+def register_torch_ops() -> None:
+    """Register torch.ops.amfls.{run_amfls, run_fixed_rbgk} for CUDA tensors."""
+    if _LIBS:
+        return
+    defined = {n: _op_exists(n) for n in ("run_amfls", "run_fixed_rbgk")}
+    if not all(defined.values()):
+        lib_def = torch.library.Library("amfls", "FRAGMENT")
+        if not defined["run_amfls"]:
+            lib_def.define(RUN_AMFLS_SCHEMA)
+        if not defined["run_fixed_rbgk"]:
+            lib_def.define(RUN_FIXED_RBGK_SCHEMA)
+        _LIBS.append(lib_def)
+    lib_impl = torch.library.Library("amfls", "IMPL")
+    for key in ("CUDA", "SparseCsrCUDA"):
+        lib_impl.impl("run_amfls", _run_amfls_impl, key)
+        lib_impl.impl("run_fixed_rbgk", _run_fixed_rbgk_impl, key)
+    _LIBS.append(lib_impl)
+
+
+def load_library(path: str | Path | None = None) -> Path:
+    """Load libamfls_gb300.so and register the torch ops (reference: binding.py:92-97)."""
+    import os
+
+    if path is not None:
+        os.environ["AMFLS_GB300_LIBRARY"] = str(Path(path).expanduser().resolve())
+    _native.load()
+    register_torch_ops()
+    return _native.library_path()
+
+
+# --------------------------------------------------------- python API ----
+
+def _check_inputs(matrix: torch.Tensor, b: torch.Tensor) -> None:
+    if matrix.device.type != "cuda" or b.device.type != "cuda":
+        raise ValueError("the GB300 binding supports CUDA tensors only")
+    if matrix.dtype != torch.float64 or b.dtype != torch.float64:
+        raise ValueError("matrix and b must use torch.float64")
+    if matrix.layout not in (torch.strided, torch.sparse_csr):
+        raise ValueError("matrix must use dense strided or sparse CSR storage")
+    if b.layout != torch.strided:
+        raise ValueError("b must use dense strided storage")
+    if matrix.ndim != 2 or b.ndim != 1 or matrix.shape[0] != b.shape[0]:
+        raise ValueError("matrix must have shape (m,n) and b must have shape (m,)")
+
+
+def _canonical_uint64_to_int64_transport(value: int, name: str) -> int:
+    if isinstance(value, bool) or not isinstance(value, int):
+        raise ValueError(f"{name} must be an integer in [0, 2**64 - 1]")
+    if value < 0 or value >= 1 << 64:
+        raise ValueError(f"{name} must be an integer in [0, 2**64 - 1]")
+    return value if value < 1 << 63 else value - (1 << 64)
+
+
+def _decode(raw) -> SolveResult:
+    if not isinstance(raw, (tuple, list)) or len(raw) != 8:
+        raise RuntimeError("AMFLS binding result must be an eight-item tuple")
+    solution, metrics, counters, timings, trace_float, trace_int, status, reason = raw
+    if metrics.shape != (21,) or counters.shape != (36,) or timings.shape != (9,):
+        raise RuntimeError("AMFLS binding result tensors have the wrong shape")
+    if trace_float.ndim != 2 or trace_float.shape[1] != 29 or \
+            tuple(trace_int.shape) != (trace_float.shape[0], 4):
+        raise RuntimeError("AMFLS binding trace tensors have the wrong shape")
+    fields = {"solution": solution}
+    m = metrics.tolist()
+    c = counters.tolist()
+    t = timings.tolist()
+    fields.update({k: float(m[i]) for i, k in enumerate(_METRIC_NAMES)})
+    fields.update({k: int(c[i]) for i, k in enumerate(_COUNTER_NAMES)})
+    fields.update({k: float(t[i]) for i, k in enumerate(_TIMING_NAMES)})
+    fields.update(trace=trace_float[:, :18], trace_float=trace_float, trace_int=trace_int,
+                  status=int(status), stop_reason=int(reason))
+    return SolveResult(**fields)
+
+
+def run_amfls(matrix: torch.Tensor, b: torch.Tensor, *, regularization: float = 0.0,
+              tolerance: float = 1e-8, failure_probability: float = 1e-6,
+              maximum_epochs: int = 0, maximum_depth: int = 0,
+              maximum_auxiliary_width: int = 0, maximum_basis_size: int = 0, seed: int = 0,
+              stream: int = 0) -> SolveResult:
+    """AMFLS on CUDA tensors (reference: python/amfls/binding.py:259-290)."""
+    _check_inputs(matrix, b)
+    register_torch_ops()
+    return _decode(torch.ops.amfls.run_amfls(
+        matrix, b, regularization, tolerance, failure_probability, maximum_epochs,
+        maximum_depth, maximum_auxiliary_width, maximum_basis_size,
+        _canonical_uint64_to_int64_transport(seed, "seed"),
+        _canonical_uint64_to_int64_transport(stream, "stream")))
+
+
+def run_fixed_rbgk(matrix: torch.Tensor, b: torch.Tensor, *, auxiliary_width: int,
+                   maximum_depth: int, maximum_basis_size: int = 0,
+                   regularization: float = 0.0, tolerance: float = 1e-8,
+                   failure_probability: float = 1e-6, seed: int = 0,
+                   stream: int = 0) -> SolveResult:
+    """Fixed-width randomized block Golub-Kahan (reference: binding.py:293-322)."""
+    _check_inputs(matrix, b)
+    register_torch_ops()
+    return _decode(torch.ops.amfls.run_fixed_rbgk(
+        matrix, b, regularization, tolerance, failure_probability, auxiliary_width,
+        maximum_depth, maximum_basis_size,
+        _canonical_uint64_to_int64_transport(seed, "seed"),
+        _canonical_uint64_to_int64_transport(stream, "stream")))

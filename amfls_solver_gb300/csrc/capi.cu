@@ -1,0 +1,218 @@
+// C ABI layer (include/amfls_gpu.h): exceptions become error codes and the
+// message is kept per thread, mirroring the reference's exception types
+// (std::invalid_argument, std::length_error, std::logic_error, ...).
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/amfls_gpu.h"
+#include "common.cuh"
+#include "controller.hpp"
+#include "csr_operator.hpp"
+#include "dense_operator.hpp"
+
+struct amfls_gpu_operator {
+    std::unique_ptr<amfls_gpu::DeviceOperator> impl;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        g_last_error.clear();
+        return AMFLS_GPU_OK;
+    } catch (const std::invalid_argument& e) {
+        g_last_error = e.what();
+        return AMFLS_GPU_INVALID_ARGUMENT;
+    } catch (const std::length_error& e) {
+        g_last_error = e.what();
+        return AMFLS_GPU_LENGTH_ERROR;
+    } catch (const std::overflow_error& e) {
+        g_last_error = e.what();
+        return AMFLS_GPU_LENGTH_ERROR;
+    } catch (const std::logic_error& e) {
+        g_last_error = e.what();
+        return AMFLS_GPU_LOGIC_ERROR;
+    } catch (const amfls_gpu::CudaError& e) {
+        g_last_error = e.what();
+        return AMFLS_GPU_CUDA_ERROR;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return AMFLS_GPU_RUNTIME_ERROR;
+    } catch (...) {
+        g_last_error = "unknown error";
+        return AMFLS_GPU_RUNTIME_ERROR;
+    }
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+amfls_gpu::SolveOptions to_options(const amfls_gpu_options* o) {
+    if (o == nullptr) throw std::invalid_argument("options must not be null");
+    amfls_gpu::SolveOptions s;
+    s.regularization = o->regularization;
+    s.tolerance = o->tolerance;
+    s.failure_probability = o->failure_probability;
+    s.maximum_epochs = o->maximum_epochs;
+    s.maximum_basis_size = o->maximum_basis_size;
+    s.seed = o->seed;
+    s.stream = o->stream;
+    s.maximum_depth = o->maximum_depth;
+    s.maximum_auxiliary_width = o->maximum_auxiliary_width;
+    s.auxiliary_width = o->auxiliary_width;
+    s.stop_early = o->stop_early != 0;
+    s.time_operators = o->time_operators != 0;
+    return s;
+}
+
+void export_result(const amfls_gpu::SolveResult& r, amfls_gpu_result* out, double* tf,
+                   int64_t* ti, int cap) {
+    if (out == nullptr) throw std::invalid_argument("result must not be null");
+    out->rows = r.rows;
+    out->cols = r.cols;
+    out->iterations = r.iterations;
+    out->depth = r.depth;
+    out->auxiliary_width = r.auxiliary_width;
+    out->basis_rank = r.basis_rank;
+    out->status = r.status;
+    out->stop_reason = r.stop_reason;
+    amfls_gpu::pack_metrics(r, out->metrics);
+    amfls_gpu::pack_counters(r, out->counters);
+    amfls_gpu::pack_timings(r, out->timings);
+    out->trace_rows = static_cast<int>(r.trace.size());
+    const int rows = std::min<int>(cap, static_cast<int>(r.trace.size()));
+    for (int i = 0; i < rows; ++i) {
+        if (tf) std::memcpy(tf + 29 * i, r.trace[i].f, sizeof(double) * 29);
+        if (ti)
+            for (int j = 0; j < 4; ++j) ti[4 * i + j] = r.trace[i].i[j];
+    }
+}
+
+const amfls_gpu::DeviceOperator& deref(const amfls_gpu_operator* op) {
+    if (op == nullptr || !op->impl) throw std::invalid_argument("operator must not be null");
+    return *op->impl;
+}
+
+}  // namespace
+
+extern "C" {
+
+void amfls_gpu_default_options(amfls_gpu_options* o) {
+    if (o == nullptr) return;
+    std::memset(o, 0, sizeof(*o));
+    o->regularization = 0.0;
+    o->tolerance = 1e-8;
+    o->failure_probability = 1e-6;
+    o->auxiliary_width = 4;
+    o->maximum_depth = 0;
+    o->stop_early = 1;
+    o->time_operators = 1;
+}
+
+const char* amfls_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int amfls_gpu_csr_operator_create(int rows, int cols, const int64_t* d_row_offsets,
+                                  const int64_t* d_column_indices, const double* d_values,
+                                  int64_t nonzeros, void* stream, amfls_gpu_operator** out) {
+    return guarded([&] {
+        if (out == nullptr) throw std::invalid_argument("output handle must not be null");
+        *out = nullptr;
+        auto h = std::make_unique<amfls_gpu_operator>();
+        h->impl = std::make_unique<amfls_gpu::CsrOperator>(
+            rows, cols, reinterpret_cast<const long long*>(d_row_offsets),
+            reinterpret_cast<const long long*>(d_column_indices), d_values, nonzeros,
+            as_stream(stream));
+        *out = h.release();
+    });
+}
+
+int amfls_gpu_dense_operator_create(int rows, int cols, const double* d_values, int column_major,
+                                    void* stream, amfls_gpu_operator** out) {
+    return guarded([&] {
+        if (out == nullptr) throw std::invalid_argument("output handle must not be null");
+        *out = nullptr;
+        auto h = std::make_unique<amfls_gpu_operator>();
+        h->impl = std::make_unique<amfls_gpu::DenseOperator>(rows, cols, d_values,
+                                                             column_major != 0, as_stream(stream));
+        *out = h.release();
+    });
+}
+
+int amfls_gpu_operator_destroy(amfls_gpu_operator* op) {
+    return guarded([&] { delete op; });
+}
+
+int amfls_gpu_operator_rows(const amfls_gpu_operator* op) {
+    return op && op->impl ? op->impl->rows() : -1;
+}
+
+int amfls_gpu_operator_cols(const amfls_gpu_operator* op) {
+    return op && op->impl ? op->impl->cols() : -1;
+}
+
+int amfls_gpu_operator_apply(const amfls_gpu_operator* op, const double* d_x, int block_cols,
+                             double* d_y, void* stream) {
+    return guarded([&] {
+        if (d_x == nullptr || d_y == nullptr || block_cols <= 0)
+            throw std::invalid_argument("apply block is invalid");
+        deref(op).apply(d_x, block_cols, d_y, as_stream(stream));
+    });
+}
+
+int amfls_gpu_operator_apply_transpose(const amfls_gpu_operator* op, const double* d_y,
+                                       int block_cols, double* d_x, void* stream) {
+    return guarded([&] {
+        if (d_x == nullptr || d_y == nullptr || block_cols <= 0)
+            throw std::invalid_argument("transpose block is invalid");
+        deref(op).apply_transpose(d_y, block_cols, d_x, as_stream(stream));
+    });
+}
+
+double amfls_gpu_operator_relative_block_product_cost(const amfls_gpu_operator* op,
+                                                      int block_cols) {
+    if (op == nullptr || !op->impl) return __builtin_huge_val();
+    return op->impl->relative_block_product_cost(block_cols);
+}
+
+int amfls_gpu_operator_validation_error_model(const amfls_gpu_operator* op,
+                                              amfls_gpu_validation_error_model* out) {
+    return guarded([&] {
+        if (out == nullptr) throw std::invalid_argument("output must not be null");
+        const auto m = deref(op).validation_error_model();
+        out->operator_norm_upper_bound = m.norm_upper;
+        out->operator_norm_lower_bound = m.norm_lower;
+        out->apply_rounding_steps = m.apply_steps;
+        out->apply_transpose_rounding_steps = m.transpose_steps;
+    });
+}
+
+int amfls_gpu_solve_amfls(const amfls_gpu_operator* op, const double* d_b,
+                          const amfls_gpu_options* options, double* d_solution,
+                          amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                          int trace_capacity, void* stream) {
+    return guarded([&] {
+        if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
+        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, to_options(options), d_solution,
+                                              as_stream(stream));
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+    });
+}
+
+int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
+                               const amfls_gpu_options* options, double* d_solution,
+                               amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                               int trace_capacity, void* stream) {
+    return guarded([&] {
+        if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
+        const auto r = amfls_gpu::solve_fixed_rbgk(deref(op), d_b, to_options(options),
+                                                   d_solution, as_stream(stream));
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+    });
+}
+
+}  // extern "C"

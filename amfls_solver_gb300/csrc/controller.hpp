@@ -1,0 +1,79 @@
+// AMFLS controller (host C++20) over the device workspace.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "device_operator.hpp"
+#include "validation.hpp"
+
+namespace amfls_gpu {
+
+// AmflsOptions (include/amfls/amfls.hpp:10-20) plus FixedRbgkOptions'
+// fields (include/amfls/fixed_rbgk.hpp:8-18) and GB300 switches.
+struct SolveOptions {
+    double regularization = 0.0;
+    double tolerance = 1e-8;
+    double failure_probability = 1e-6;
+    int maximum_epochs = 0;
+    int maximum_basis_size = 0;
+    std::uint64_t seed = 0;
+    std::uint64_t stream = 0;
+    int maximum_depth = 0;
+    int maximum_auxiliary_width = 0;
+    int auxiliary_width = 4;  // fixed RBGK only
+    bool stop_early = true;   // fixed RBGK only
+    bool time_operators = true;
+};
+
+// RunStatistics (include/amfls/least_squares_result.hpp:57-109).
+struct Statistics {
+    long long a_columns = 0, at_columns = 0, a_block_calls = 0, at_block_calls = 0;
+    long long search_a_columns = 0, search_at_columns = 0;
+    long long validation_a_columns = 0, validation_at_columns = 0;
+    long long sketch_a_columns = 0, sketch_at_columns = 0, sketch_a_block_calls = 0,
+              sketch_at_block_calls = 0;
+    long long iterative_a_columns = 0, iterative_at_columns = 0, iterative_a_block_calls = 0,
+              iterative_at_block_calls = 0;
+    long long gaussian_random_columns = 0, gaussian_random_values = 0;
+    double total_seconds = 0.0, a_seconds = 0.0, at_seconds = 0.0;
+    double orthogonalization_seconds = 0.0, projected_solve_seconds = 0.0, validation_seconds = 0.0;
+    long long search_a_block_calls = 0, search_at_block_calls = 0;
+    long long validation_a_block_calls = 0, validation_at_block_calls = 0;
+    long long base_validation_a_columns = 0, base_validation_at_columns = 0;
+    long long base_validation_a_block_calls = 0, base_validation_at_block_calls = 0;
+    long long ridge_correction_a_columns = 0, ridge_correction_at_columns = 0;
+    long long ridge_correction_a_block_calls = 0, ridge_correction_at_block_calls = 0;
+    double base_validation_seconds = 0.0, ridge_correction_validation_seconds = 0.0;
+    long long gaussian_random_block_requests = 0;
+    // GB300 extras (not in the reference's tensors)
+    long long projected_rank_flags = 0;
+};
+
+struct TraceRow {
+    double f[29];
+    long long i[4];
+};
+
+// LeastSquaresResult (include/amfls/least_squares_result.hpp:162-229); the
+// solution is written to the caller's device buffer.
+struct SolveResult {
+    int rows = 0, cols = 0, iterations = 0, depth = 0, auxiliary_width = 0, basis_rank = 0;
+    ValidationOutput v{};
+    int status = 1, stop_reason = 3;
+    Statistics statistics;
+    std::vector<TraceRow> trace;
+};
+
+SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const SolveOptions& options,
+                        double* d_solution, cudaStream_t stream);
+
+SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b,
+                             const SolveOptions& options, double* d_solution, cudaStream_t stream);
+
+// Result tensors in the torch binding's layout (bindings/torch/result_tensors.hpp:12-156).
+void pack_metrics(const SolveResult& r, double out[21]);
+void pack_counters(const SolveResult& r, long long out[36]);
+void pack_timings(const SolveResult& r, double out[9]);
+
+}  // namespace amfls_gpu

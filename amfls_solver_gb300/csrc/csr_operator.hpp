@@ -1,0 +1,67 @@
+// FP64 CSR operator on the device (see csr_operator.cu).
+#pragma once
+
+#include <memory>
+
+#include "device_operator.hpp"
+
+namespace amfls_gpu {
+
+class CsrOperator final : public DeviceOperator {
+public:
+    // The CSR arrays are device pointers in the reference's layout: int64 row
+    // offsets (rows+1), int64 column indices and FP64 values (nnz).  They are
+    // copied and validated; the caller may free them afterwards.
+    // `elems_per_lane` sets the row-length binning (lanes per row ~ len / it).
+    CsrOperator(int rows, int cols, const long long* d_offsets, const long long* d_indices,
+                const double* d_values, long long nnz, cudaStream_t stream,
+                int elems_per_lane = 4);
+    ~CsrOperator() override;
+    CsrOperator(const CsrOperator&) = delete;
+    CsrOperator& operator=(const CsrOperator&) = delete;
+
+    int rows() const override { return rows_; }
+    int cols() const override { return cols_; }
+    int kind() const override { return 0; }
+    long long nonzeros() const { return nnz_; }
+    long long max_row_nonzeros() const { return max_row_nnz_; }
+    long long max_col_nonzeros() const { return max_col_nnz_; }
+
+    void apply(const double* x, int block_cols, double* y, cudaStream_t s) const override;
+    void apply_transpose(const double* y, int block_cols, double* x,
+                         cudaStream_t s) const override;
+    ValidationModel validation_error_model() const override { return model_; }
+    bool supports_validation_refinement() const override { return true; }
+    void apply_refined(const double* x_hi, const double* x_lo, double* y_hi, double* y_lo,
+                       int* finite, cudaStream_t s) const override;
+    void apply_transpose_refined(const double* y_hi, const double* y_lo, double* x_hi,
+                                 double* x_lo, int* finite, cudaStream_t s) const override;
+    bool product1(bool transpose, const double* x, const Epilogue& ep,
+                  cudaStream_t s) const override;
+
+private:
+    struct Side;
+    void build(const long long* d_off, const long long* d_idx, const double* d_val,
+               cudaStream_t stream);
+    void build_bins(Side& s, const int* d_bins, cudaStream_t stream);
+    void fill_ids(int* ids, long long n, cudaStream_t stream);
+    void product(bool transpose, const double* x, int block_cols, double* y,
+                 cudaStream_t stream) const;
+    void refined(bool transpose, const double* x_hi, const double* x_lo, double* y_hi,
+                 double* y_lo, int* finite, cudaStream_t stream) const;
+    void release();
+
+    int rows_;
+    int cols_;
+    long long nnz_;
+    int elems_per_lane_;
+    long long max_row_nnz_ = 0;
+    long long max_col_nnz_ = 0;
+    ValidationModel model_;
+    std::unique_ptr<Side> a_;
+    std::unique_ptr<Side> t_;
+    double* scratch_ = nullptr;
+    unsigned* counter_ = nullptr;
+};
+
+}  // namespace amfls_gpu

@@ -1,0 +1,352 @@
+// Dense FP64 operator: Y = A X and X = A^T Y with A resident in HBM.
+//
+// Replaces DenseOperator (src/algorithms/mathematics/operators/dense_operator.cpp:20-185,
+// column-major, dgemm) and RowMajorDenseOperator
+// (row_major_dense_operator.cpp:106-258, row-major, the torch path).
+// The product along the contiguous dimension is a warp-per-output dot
+// product; the product across it keeps one output per thread (coalesced
+// over the contiguous dimension) and splits the long dimension into chunks
+// whose partial sums a second kernel adds in a fixed order, so results are
+// deterministic.  The certified norm model and the rounding-step counts
+// (2 cols + 2 for A, 2 rows + 2 for A^T) follow the reference; row and column
+// sums of |a_ij| are accumulated in the reference's storage order.
+// On GB300 FP64 issue rate, not HBM bandwidth, bounds these kernels
+// (2 flops per 8-byte element against a ~0.18 flop/byte FP64 ridge).
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+#include "common.cuh"
+#include "dd.cuh"
+#include "dense_operator.hpp"
+#include "epilogue.cuh"
+#include "fp_bounds.cuh"
+
+namespace amfls_gpu {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTargetBlocks = 152 * 8;
+
+// out[o] = sum_i A(o, i) x(i) where o runs over the strided dimension:
+// element (o, i) at a[o * ld_o + i * ld_i] with ld_i == 1 (contiguous).
+__global__ void dot_rows_kernel(const double* __restrict__ a, long long ld, int outer, int inner,
+                                const double* __restrict__ x, double* y, const int* guard) {
+    if (guard && *guard == 0) return;
+    const int lane = threadIdx.x & 31;
+    for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < outer;
+         w += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const double* row = a + w * ld;
+        double acc = 0.0;
+        for (int i = lane; i < inner; i += 32) acc = fma(row[i], __ldg(x + i), acc);
+        acc = warp_sum(acc);
+        if (lane == 0) y[w] = acc;
+    }
+}
+
+// partial[c][o] = sum_{i in chunk c} A(i, o) x(i): A(i, o) at a[i * ld + o]
+__global__ void sum_cols_kernel(const double* __restrict__ a, long long ld, int outer, int inner,
+                                int chunk, const double* __restrict__ x, double* partial,
+                                const int* guard) {
+    if (guard && *guard == 0) return;
+    const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (o >= outer) return;
+    const int i0 = c * chunk, i1 = min(inner, i0 + chunk);
+    double acc = 0.0;
+    for (int i = i0; i < i1; ++i) acc = fma(a[(long long)i * ld + o], __ldg(x + i), acc);
+    partial[(long long)c * outer + o] = acc;
+}
+
+__global__ void add_chunks_kernel(const double* partial, int chunks, int outer, double* y,
+                                  const int* guard) {
+    if (guard && *guard == 0) return;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < outer;
+         o += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < chunks; ++c) s += partial[(long long)c * outer + o];
+        y[o] = s;
+    }
+}
+
+// double-double variants for the validation refinement
+__global__ void dd_dot_rows_kernel(const double* __restrict__ a, long long ld, int outer,
+                                   int inner, const double* x_hi, const double* x_lo, double* y_hi,
+                                   double* y_lo, int* finite) {
+    const int lane = threadIdx.x & 31;
+    for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < outer;
+         w += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const double* row = a + w * ld;
+        dd acc{0.0, 0.0};
+        for (int i = lane; i < inner; i += 32)
+            acc = dd_add(acc, dd_mul_d(dd{x_hi[i], x_lo ? x_lo[i] : 0.0}, row[i]));
+        for (int o = 16; o > 0; o >>= 1) acc = dd_add(acc, dd_shfl_xor(acc, o));
+        if (lane == 0) {
+            y_hi[w] = acc.hi;
+            y_lo[w] = acc.lo;
+            if (!isfinite(acc.hi) || !isfinite(acc.lo)) atomicAnd(finite, 0);
+        }
+    }
+}
+
+__global__ void dd_sum_cols_kernel(const double* __restrict__ a, long long ld, int outer,
+                                   int inner, const double* x_hi, const double* x_lo,
+                                   double* y_hi, double* y_lo, int* finite) {
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < outer;
+         o += (long long)gridDim.x * blockDim.x) {
+        dd acc{0.0, 0.0};
+        for (int i = 0; i < inner; ++i)
+            acc = dd_add(acc, dd_mul_d(dd{x_hi[i], x_lo ? x_lo[i] : 0.0}, a[(long long)i * ld + o]));
+        y_hi[o] = acc.hi;
+        y_lo[o] = acc.lo;
+        if (!isfinite(acc.hi) || !isfinite(acc.lo)) atomicAnd(finite, 0);
+    }
+}
+
+// ---- norm model: sequential sums in storage order (outer loop = storage-major)
+__device__ __forceinline__ void atomic_max_pos(double* addr, double v) {
+    atomicMax(reinterpret_cast<unsigned long long*>(addr),
+              (unsigned long long)__double_as_longlong(v));
+}
+
+// acc: [0] max outer-sum upper, [1] max two-norm lower, [2] max entry,
+//      [3] max inner-sum upper, [4] nonfinite flag
+__global__ void model_outer_kernel(const double* a, int outer, int inner, double* acc,
+                                   double* frob_partials, unsigned* counter, double* frob_out) {
+    __shared__ double scratch[32];
+    double frob = 0.0;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < outer;
+         o += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0, q = 0.0, mx = 0.0;
+        bool bad = false;
+        for (int i = 0; i < inner; ++i) {
+            const double m = fabs(a[o * (long long)inner + i]);
+            if (!isfinite(m)) {
+                bad = true;
+                continue;
+            }
+            mx = fmax(mx, m);
+            s += m;
+            q = fma(m, m, q);
+        }
+        if (bad) atomic_max_pos(&acc[4], 1.0);
+        atomic_max_pos(&acc[0], fpb::sum_upper(s, inner, true));
+        atomic_max_pos(&acc[1], fpb::down_sqrt(fpb::sum_lower(q, inner)));
+        atomic_max_pos(&acc[2], mx);
+        frob = __dadd_ru(frob, fpb::sum_upper(q, inner, false));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) frob = __dadd_ru(frob, __shfl_xor_sync(0xffffffffu, frob, o));
+    if (lane == 0) scratch[warp] = frob;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = __dadd_ru(t, scratch[w]);
+        frob_partials[blockIdx.x] = t;
+    }
+    if (arrive_last(counter, gridDim.x) && threadIdx.x == 0) {
+        double t = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) t = __dadd_ru(t, frob_partials[b]);
+        *frob_out = fpb::widen_up(t);
+    }
+}
+
+// per inner index: sums over the outer dimension in order; Frobenius terms
+// rounded upward per index, then summed upward by the last block
+__global__ void model_inner_kernel(const double* a, int outer, int inner, double* acc,
+                                   double* frob_partials, unsigned* counter, double* frob_out) {
+    __shared__ double scratch[32];
+    double frob = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < inner;
+         i += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0, q = 0.0;
+        for (int o = 0; o < outer; ++o) {
+            const double m = fabs(a[(long long)o * inner + i]);
+            if (!isfinite(m)) continue;
+            s += m;
+            q = fma(m, m, q);
+        }
+        atomic_max_pos(&acc[3], fpb::sum_upper(s, outer, true));
+        atomic_max_pos(&acc[1], fpb::down_sqrt(fpb::sum_lower(q, outer)));
+        frob = __dadd_ru(frob, fpb::sum_upper(q, outer, false));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) frob = __dadd_ru(frob, __shfl_xor_sync(0xffffffffu, frob, o));
+    if (lane == 0) scratch[warp] = frob;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = __dadd_ru(t, scratch[w]);
+        frob_partials[blockIdx.x] = t;
+    }
+    if (arrive_last(counter, gridDim.x) && threadIdx.x == 0) {
+        double t = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) t = __dadd_ru(t, frob_partials[b]);
+        *frob_out = fpb::widen_up(t);
+    }
+}
+
+__global__ void model_finish_kernel(const double* acc, const double* frob2, int row_major,
+                                    double* model) {
+    // row-major: outer = rows -> acc[0] is the row-sum bound (||A||_inf),
+    // acc[3] the column-sum bound (||A||_1); column-major the reverse
+    const double row_sum = row_major ? acc[0] : acc[3];
+    const double col_sum = row_major ? acc[3] : acc[0];
+    double upper = fpb::kInf;
+    double lower = 0.0;
+    if (acc[4] == 0.0) {
+        const double one_inf = fpb::up_mul(fpb::up_sqrt(col_sum), fpb::up_sqrt(row_sum));
+        upper = fmin(one_inf, fpb::up_sqrt(*frob2));
+        lower = fmax(acc[2], acc[1]);
+    }
+    if (!isfinite(upper) || lower > upper) {
+        upper = fpb::kInf;
+        lower = 0.0;
+    }
+    model[0] = upper;
+    model[1] = lower;
+}
+
+__global__ void epilogue_kernel(const double* __restrict__ t, long long n, Epilogue ep,
+                                double* partials, unsigned* counter) {
+    if (ep.guard && *ep.guard == 0) return;
+    double sq_t = 0.0, sq_out = 0.0, dot = 0.0, mx_t = 0.0, mx_out = 0.0;
+    int nonfin = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        epilogue_row(ep, (int)i, t[i], sq_t, sq_out, dot, mx_t, mx_out, nonfin);
+    finish_reduction(ep, sq_t, sq_out, dot, mx_t, mx_out, nonfin, partials, counter);
+}
+
+int grid_1d(long long items) {
+    return (int)std::max<long long>(1, std::min<long long>(kTargetBlocks, (items + 255) / 256));
+}
+
+}  // namespace
+
+void run_epilogue(const double* t, long long n, const Epilogue& ep, double* partials,
+                  unsigned* counter, cudaStream_t s) {
+    epilogue_kernel<<<grid_1d(n), kThreads, 0, s>>>(t, n, ep, partials, counter);
+    AMFLS_CUDA(cudaGetLastError());
+}
+
+DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool column_major,
+                             cudaStream_t stream)
+    : rows_(rows), cols_(cols), a_(d_values), column_major_(column_major) {
+    if (rows <= 0 || cols <= 0 || d_values == nullptr)
+        throw std::invalid_argument("dense operator input is invalid");
+    const int outer = column_major ? cols : rows;
+    const int inner = column_major ? rows : cols;
+    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kTargetBlocks + 64)));
+    AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * 8));
+    AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * 8, stream));
+    AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows, cols)));
+    // w: acc[5] | frob(inner) | model[2] | frob(outer) | partials (inner) | partials (outer)
+    double* w = nullptr;
+    const int ig = grid_1d(inner), og = grid_1d(outer);
+    AMFLS_CUDA(cudaMallocAsync(&w, sizeof(double) * (9 + ig + og), stream));
+    AMFLS_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * (9 + ig + og), stream));
+    model_outer_kernel<<<og, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9 + ig, counter_ + 2,
+                                                    w + 8);
+    model_inner_kernel<<<ig, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9, counter_, w + 5);
+    // the reference's Frobenius bound sums column square sums: the inner
+    // index for row-major storage, the outer one for column-major
+    model_finish_kernel<<<1, 1, 0, stream>>>(w, column_major ? w + 8 : w + 5,
+                                             column_major ? 0 : 1, w + 6);
+    AMFLS_CUDA(cudaGetLastError());
+    double model[2];
+    AMFLS_CUDA(cudaMemcpyAsync(model, w + 6, sizeof(model), cudaMemcpyDeviceToHost, stream));
+    AMFLS_CUDA(cudaStreamSynchronize(stream));
+    AMFLS_CUDA(cudaFreeAsync(w, stream));
+    model_.norm_upper = model[0];
+    model_.norm_lower = model[1];
+    model_.apply_steps = 2LL * cols + 2LL;
+    model_.transpose_steps = 2LL * rows + 2LL;
+}
+
+DenseOperator::~DenseOperator() {
+    cudaFree(partials_);
+    cudaFree(tmp_);
+    cudaFree(scratch_);
+    cudaFree(counter_);
+}
+
+void DenseOperator::product(bool transpose, const double* x, double* y, const int* guard,
+                            cudaStream_t s) const {
+    // y has length rows (apply) or cols (transpose)
+    const int out_n = transpose ? cols_ : rows_;
+    const int in_n = transpose ? rows_ : cols_;
+    // contiguous dimension: row-major rows are contiguous (apply = dot rows);
+    // column-major columns are contiguous (transpose = dot rows of A^T)
+    const bool dot = column_major_ == transpose;
+    const long long ld = column_major_ ? rows_ : cols_;
+    if (dot) {
+        const long long warps = out_n;
+        const int grid = (int)std::max<long long>(1, std::min<long long>(kTargetBlocks * 2, (warps + 7) / 8));
+        dot_rows_kernel<<<grid, kThreads, 0, s>>>(a_, ld, out_n, in_n, x, y, guard);
+    } else {
+        const int oblocks = (out_n + 255) / 256;
+        int chunks = std::max(1, std::min((kTargetBlocks + oblocks - 1) / oblocks, (in_n + 63) / 64));
+        const int chunk = (in_n + chunks - 1) / chunks;
+        chunks = (in_n + chunk - 1) / chunk;
+        const long long need = (long long)chunks * out_n;
+        if (need > partial_cap_) {
+            auto* self = const_cast<DenseOperator*>(this);
+            AMFLS_CUDA(cudaStreamSynchronize(s));
+            cudaFree(self->partials_);
+            AMFLS_CUDA(cudaMalloc(&self->partials_, sizeof(double) * need));
+            self->partial_cap_ = need;
+        }
+        sum_cols_kernel<<<dim3(oblocks, chunks), kThreads, 0, s>>>(a_, ld, out_n, in_n, chunk, x,
+                                                                   partials_, guard);
+        add_chunks_kernel<<<grid_1d(out_n), kThreads, 0, s>>>(partials_, chunks, out_n, y, guard);
+    }
+    AMFLS_CUDA(cudaGetLastError());
+}
+
+void DenseOperator::apply(const double* x, int block_cols, double* y, cudaStream_t s) const {
+    if (x == nullptr || y == nullptr || block_cols <= 0)
+        throw std::invalid_argument("dense apply block is invalid");
+    for (int c = 0; c < block_cols; ++c) product(false, x + (long long)c * cols_, y + (long long)c * rows_, nullptr, s);
+}
+
+void DenseOperator::apply_transpose(const double* y, int block_cols, double* x,
+                                    cudaStream_t s) const {
+    if (x == nullptr || y == nullptr || block_cols <= 0)
+        throw std::invalid_argument("dense transpose block is invalid");
+    for (int c = 0; c < block_cols; ++c) product(true, y + (long long)c * rows_, x + (long long)c * cols_, nullptr, s);
+}
+
+bool DenseOperator::product1(bool transpose, const double* x, const Epilogue& ep,
+                             cudaStream_t s) const {
+    product(transpose, x, tmp_, ep.guard, s);
+    run_epilogue(tmp_, transpose ? cols_ : rows_, ep, ep.partials ? ep.partials : scratch_,
+                 ep.counter ? ep.counter : counter_ + 1, s);
+    return true;
+}
+
+void DenseOperator::apply_refined(const double* x_hi, const double* x_lo, double* y_hi,
+                                  double* y_lo, int* finite, cudaStream_t s) const {
+    if (!column_major_) {
+        dd_dot_rows_kernel<<<grid_1d((long long)rows_ * 32), kThreads, 0, s>>>(
+            a_, cols_, rows_, cols_, x_hi, x_lo, y_hi, y_lo, finite);
+    } else {
+        dd_sum_cols_kernel<<<grid_1d(rows_), kThreads, 0, s>>>(a_, rows_, rows_, cols_, x_hi,
+                                                               x_lo, y_hi, y_lo, finite);
+    }
+    AMFLS_CUDA(cudaGetLastError());
+}
+
+void DenseOperator::apply_transpose_refined(const double* y_hi, const double* y_lo, double* x_hi,
+                                            double* x_lo, int* finite, cudaStream_t s) const {
+    if (column_major_) {
+        dd_dot_rows_kernel<<<grid_1d((long long)cols_ * 32), kThreads, 0, s>>>(
+            a_, rows_, cols_, rows_, y_hi, y_lo, x_hi, x_lo, finite);
+    } else {
+        dd_sum_cols_kernel<<<grid_1d(cols_), kThreads, 0, s>>>(a_, cols_, cols_, rows_, y_hi,
+                                                               y_lo, x_hi, x_lo, finite);
+    }
+    AMFLS_CUDA(cudaGetLastError());
+}
+
+}  // namespace amfls_gpu

@@ -1,0 +1,102 @@
+// Device-side MatrixOperator contract.
+//
+// Mirrors include/amfls/matrix_operator.hpp:29-89 of the reference with
+// device pointers: apply / apply_transpose act on column-major blocks
+// X (cols x s) and Y (rows x s) resident in GPU memory, asynchronously on a
+// CUDA stream.  relative_block_product_cost and validation_error_model keep
+// their meaning; the extended-precision validation products of the
+// reference (long double, matrix_operator.hpp:70-88) become double-double
+// products here (apply_refined / apply_transpose_refined).
+//
+// Built-in operators also implement `product1`, a single-column product with
+// a fused epilogue and a device-side guard flag.  The solver uses it so that
+// an enqueued level does no work once the device state says the process
+// must stop, and so that the norms and dot products the level needs come
+// out of the same pass over the operator.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <limits>
+
+namespace amfls_gpu {
+
+struct ValidationModel {
+    double norm_upper = std::numeric_limits<double>::infinity();
+    double norm_lower = 0.0;
+    long long apply_steps = 0;
+    long long transpose_steps = 0;
+};
+
+// Reductions produced by a fused epilogue (written by the last block).
+struct RedResult {
+    double sq_t;       // sum t_i^2
+    double sq_out;     // sum out_i^2
+    double dot;        // sum out_i * dot_vec_i
+    double max_t;      // max |t_i|
+    double max_out;    // max |out_i|
+    int nonfinite;     // count of nonfinite t_i or out_i
+    int pad;
+};
+
+// t_i is the i-th entry of the product.  Then
+//   out_i = t_i - (*coef) * sub[i * sub_stride]         if sub != nullptr
+//   out_i = fma(lambda, fma_vec[i], t_i)                 if fma_vec != nullptr
+//   out_i = t_i - minus_vec[i]                           if minus_vec != nullptr
+//   out_i = t_i                                          otherwise
+struct Epilogue {
+    double* t_out = nullptr;
+    double* out = nullptr;
+    const double* sub = nullptr;
+    long long sub_stride = 1;
+    const double* coef = nullptr;
+    const double* fma_vec = nullptr;
+    double lambda = 0.0;
+    const double* minus_vec = nullptr;
+    const double* dot_vec = nullptr;
+    RedResult* red = nullptr;
+    const int* guard = nullptr;  // skip the launch's work when *guard == 0
+    // Scratch for the cross-block reduction (one slot of 6 doubles per block
+    // and a ticket counter that must start at zero).  When null the operator
+    // uses its own, which serialises fused products on one operator.
+    double* partials = nullptr;
+    unsigned* counter = nullptr;
+};
+
+class DeviceOperator {
+public:
+    virtual ~DeviceOperator() = default;
+    virtual int rows() const = 0;
+    virtual int cols() const = 0;
+    virtual void apply(const double* x, int block_cols, double* y, cudaStream_t s) const = 0;
+    virtual void apply_transpose(const double* y, int block_cols, double* x,
+                                 cudaStream_t s) const = 0;
+    virtual double relative_block_product_cost(int block_cols) const {
+        return block_cols > 0 ? static_cast<double>(block_cols)
+                              : std::numeric_limits<double>::infinity();
+    }
+    virtual ValidationModel validation_error_model() const { return {}; }
+    virtual bool supports_validation_refinement() const { return false; }
+    // Double-double validation products.  Inputs and outputs are (hi, lo)
+    // pairs; `finite` receives 0 when a nonfinite value appeared.
+    virtual void apply_refined(const double* x_hi, const double* x_lo, double* y_hi,
+                               double* y_lo, int* finite, cudaStream_t s) const {
+        (void)x_hi; (void)x_lo; (void)y_hi; (void)y_lo; (void)finite; (void)s;
+    }
+    virtual void apply_transpose_refined(const double* y_hi, const double* y_lo, double* x_hi,
+                                         double* x_lo, int* finite, cudaStream_t s) const {
+        (void)y_hi; (void)y_lo; (void)x_hi; (void)x_lo; (void)finite; (void)s;
+    }
+    // Fused single-column product; returns false when the operator has none.
+    virtual bool product1(bool transpose, const double* x, const Epilogue& ep,
+                          cudaStream_t s) const {
+        (void)transpose; (void)x; (void)ep; (void)s;
+        return false;
+    }
+    // Storage kind for diagnostics: 0 CSR, 1 row-major dense, 2 column-major
+    // dense, 3 custom callbacks.
+    virtual int kind() const = 0;
+};
+
+}  // namespace amfls_gpu

@@ -1,0 +1,60 @@
+// Fused epilogue of single-column products (see device_operator.hpp).
+#pragma once
+
+#include "common.cuh"
+#include "device_operator.hpp"
+
+namespace amfls_gpu {
+
+__device__ __forceinline__ void epilogue_row(const Epilogue& ep, int row, double t, double& sq_t,
+                                             double& sq_out, double& dot, double& mx_t,
+                                             double& mx_out, int& nonfin) {
+    double out = t;
+    if (ep.sub) out = t - (*ep.coef) * ep.sub[(long long)row * ep.sub_stride];
+    else if (ep.fma_vec) out = fma(ep.lambda, ep.fma_vec[row], t);
+    else if (ep.minus_vec) out = t - ep.minus_vec[row];
+    if (ep.t_out) ep.t_out[row] = t;
+    if (ep.out) ep.out[row] = out;
+    if (ep.red) {
+        sq_t = fma(t, t, sq_t);
+        sq_out = fma(out, out, sq_out);
+        if (ep.dot_vec) dot = fma(out, ep.dot_vec[row], dot);
+        mx_t = fmax(mx_t, fabs(t));
+        mx_out = fmax(mx_out, fabs(out));
+        if (!isfinite(t) || !isfinite(out)) ++nonfin;
+    }
+}
+
+__device__ inline void finish_reduction(const Epilogue& ep, double sq_t, double sq_out, double dot,
+                                 double mx_t, double mx_out, int nonfin, double* partials,
+                                 unsigned* counter) {
+    __shared__ double scratch[32];
+    if (!ep.red) return;
+    double v[6] = {sq_t, sq_out, dot, mx_t, mx_out, (double)nonfin};
+    double r[6];
+    for (int i = 0; i < 6; ++i)
+        r[i] = (i == 3 || i == 4) ? block_max(v[i], scratch) : block_sum(v[i], scratch);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < 6; ++i) partials[blockIdx.x * 6 + i] = r[i];
+    if (arrive_last(counter, gridDim.x)) {
+        for (int i = 0; i < 6; ++i) {
+            double a = (i == 3 || i == 4) ? 0.0 : 0.0;
+            for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+                const double p = partials[b * 6 + i];
+                a = (i == 3 || i == 4) ? fmax(a, p) : a + p;
+            }
+            r[i] = (i == 3 || i == 4) ? block_max(a, scratch) : block_sum(a, scratch);
+        }
+        if (threadIdx.x == 0) {
+            ep.red->sq_t = r[0];
+            ep.red->sq_out = r[1];
+            ep.red->dot = r[2];
+            ep.red->max_t = r[3];
+            ep.red->max_out = r[4];
+            ep.red->nonfinite = (int)r[5];
+        }
+    }
+}
+
+
+}  // namespace amfls_gpu

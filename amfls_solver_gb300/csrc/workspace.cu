@@ -1,0 +1,876 @@
+// Device block Golub-Kahan workspace (see workspace.hpp for the layout).
+//
+// One width-one level (krylov_workspace.cpp:589-831) is the kernel chain
+//   begin        decide on the device whether the level runs (can_advance,
+//                depth target); reset the step audit
+//   A^T u        fused SpMV^T: r = A^T u - beta v_prev, ||A^T u||, ||r||
+//   V^T r        c1, per-panel partials reduced by the last block per panel
+//   r -= V c1    with ||r||; its last block takes the DGKS decision
+//                (second pass only if ||r_after|| < sqrt(1/2) ||r_before||,
+//                krylov_workspace.cpp:152-165) and, when no second pass is
+//                needed, the rank decision against the cutoff
+//                64 eps max(m,n,k,1) ||A^T u|| (krylov_workspace.cpp:63-80)
+//   [V^T r, r -= V c2]   only when the device flag asks for it
+//   normalise    v = r / ||r|| into V's new column and a contiguous copy
+//   A v          fused SpMV: y = A v - ||r|| u, ||A v||, ||y||, u.y
+//   left pass    y -= (u.y) u with ||y||, u.y, y.b; DGKS and rank decision,
+//                T column (alpha = ||r|| + u.y, beta = ||y||), g = u'.b
+//   [left pass]  second DGKS pass when flagged
+//   normalise    u' = y / ||y||
+// Every kernel reads the device flag `go` and does nothing once the level
+// (or an earlier one) stopped, so a whole run of levels up to the next
+// checkpoint is enqueued without a host round trip.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "common.cuh"
+#include "vector_ops.hpp"
+#include "workspace.hpp"
+
+namespace amfls_gpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr double kEps = 2.220446049250313e-16;
+constexpr int kGemvTargetBlocks = 152 * 16;
+
+enum Hook { kHookNone = 0, kHookRightPass1 = 1, kHookRightPass2 = 2 };
+
+__device__ inline bool dfinite(double v) { return isfinite(v); }
+
+// Rank decision for the width-one right residual (krylov_workspace.cpp:197-310,
+// scalar branch) after its final projection pass.
+__device__ void decide_right(DevState* st, int m, int n) {
+    const double scale = st->right_scale;
+    const double after = st->norm_after;
+    const int k = st->k;
+    const int dim = max(max(1, m), max(n, max(k, 1)));
+    const double cutoff = (scale >= 0.0 && dfinite(scale)) ? 64.0 * kEps * dim * scale
+                                                           : __builtin_huge_val();
+    const bool finite = dfinite(scale) && dfinite(after) && !st->coeff_nonfinite;
+    const int max_rank = min(1, st->basis_limit - k);  // combined width is one
+    StepAudit& a = st->audit;
+    int rank = 0;
+    double discarded = after, tracked = 0.0;
+    bool positive = false;
+    if (!finite) {
+        discarded = __builtin_huge_val();
+        tracked = __builtin_huge_val();  // tracked prefix = active width = 1
+    } else if (max_rank == 0) {
+        tracked = after;
+    } else if (after > cutoff) {
+        rank = 1;
+        discarded = 0.0;
+    } else if (after > 0.0) {
+        positive = true;
+        tracked = after;
+    }
+    a.retained_right_width = rank;
+    a.right_rank_cutoff = cutoff;
+    a.right_discarded_residual_norm = discarded;
+    a.right_active_discarded_residual_norm = tracked;
+    a.right_positive_finite_below_cutoff = positive;
+    a.right_nonfinite_residual = !finite;
+    a.right_rank_loss = rank < max_rank;
+    a.right_basis_cap_truncation = max_rank < 1;
+    const bool truncated = a.right_rank_loss && positive && tracked > 0.0;
+    if (truncated || !finite) st->reliable = 0;
+    st->right_rank = rank;
+    if (rank == 0) {
+        st->left_width = 0;
+        st->active_first = st->rows_t;
+        st->prev_right_first = k;
+        st->prev_right_width = 0;
+        st->coupling = 0.0;
+        st->level_ok = 0;
+        st->go = 0;
+        return;
+    }
+    st->right_factor = after;
+    st->inv_right = 1.0 / after;
+    st->search_a_calls += 1;
+    st->search_a_columns += 1;
+}
+
+// Rank decision of the left residual and the T / g update
+// (krylov_workspace.cpp:736-830).
+__device__ void decide_left(DevState* st, int m, int n, double* alpha, double* beta, double* g) {
+    const double scale = st->left_scale;
+    const double after = st->left_norm;
+    const int dim = max(max(1, m), n);
+    const double cutoff = (scale >= 0.0 && dfinite(scale)) ? 64.0 * kEps * dim * scale
+                                                           : __builtin_huge_val();
+    const bool finite = dfinite(scale) && dfinite(after) && dfinite(st->left_coeff);
+    const int old_left = st->rows_t;
+    const int max_rank = min(min(1, m - old_left), st->basis_limit + 1 - old_left);
+    StepAudit& a = st->audit;
+    int rank = 0;
+    double discarded = after;
+    bool positive = false;
+    if (!finite) {
+        discarded = __builtin_huge_val();
+    } else if (max_rank <= 0) {
+        // nothing retained, nothing tracked
+    } else if (after > cutoff) {
+        rank = 1;
+        discarded = 0.0;
+    } else if (after > 0.0) {
+        positive = true;
+    }
+    a.retained_next_left_width = rank;
+    a.left_rank_cutoff = cutoff;
+    a.left_discarded_residual_norm = discarded;
+    a.left_positive_finite_below_cutoff = positive;
+    a.left_nonfinite_residual = !finite;
+    a.left_rank_loss = rank < max_rank;
+    a.left_basis_cap_truncation = max_rank < 1;
+    const bool truncated = (a.left_rank_loss && positive);
+    if (truncated || !finite) st->reliable = 0;
+    if (!finite) {
+        st->level_ok = 0;
+        st->go = 0;
+        return;
+    }
+    const int k_old = st->k;
+    alpha[k_old] = st->right_factor + st->left_coeff;  // active coupling + coefficient
+    beta[k_old] = rank ? after : 0.0;
+    if (rank) {
+        st->inv_left = 1.0 / after;
+        g[old_left] = st->b_dot * st->inv_left;
+    }
+    st->left_rank = rank;
+    st->k = k_old + 1;
+    st->active_first = old_left;
+    st->rows_t = old_left + rank;
+    st->left_width = rank;
+    st->prev_right_first = k_old;
+    st->prev_right_width = 1;
+    st->coupling = after;
+    st->depth += 1;
+    st->level_ok = 1;
+    st->levels_run += 1;
+    a.basis_rank_after = k_old + 1;
+    if (!rank) st->go = 0;  // nothing to normalise; the process stops here
+}
+
+__global__ void level_begin_kernel(DevState* st, int target_depth) {
+    if (threadIdx.x != 0) return;
+    const bool go = st->reliable && (st->left_width + st->pending > 0) &&
+                    st->k < st->basis_limit && st->depth < target_depth;
+    st->go = go ? 1 : 0;
+    if (!go) return;
+    StepAudit a;
+    memset(&a, 0, sizeof(a));
+    a.left_input_width = st->left_width + st->pending;
+    a.basis_rank_before = st->k;
+    a.basis_rank_after = st->k;
+    st->audit = a;
+    st->coupling_eff = (st->prev_right_width > 0 && st->left_width > 0) ? st->coupling : 0.0;
+    st->second_pass = 0;
+    st->right_rank = 0;
+    st->left_rank = 0;
+    st->coeff_nonfinite = 0;
+    st->level_ok = 0;
+    st->search_at_calls += 1;
+    st->search_at_columns += st->left_width + st->pending;
+}
+
+// after A^T u: scale and norm_before from the fused reduction
+__global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, int n,
+                                    int no_projection) {
+    if (threadIdx.x != 0 || !st->go) return;
+    st->right_scale = red->nonfinite ? __builtin_nan("") : sqrt(red->sq_t);
+    st->norm_before = red->nonfinite ? __builtin_nan("") : sqrt(red->sq_out);
+    if (no_projection) {  // empty basis: no pass, the norm is the block's norm
+        st->norm_after = st->norm_before;
+        decide_right(st, m, n);
+    }
+}
+
+// c = V^T r, masked to k columns.  grid (panels, chunks); partials [P][C][32].
+__global__ void __launch_bounds__(kThreads)
+vt_r_kernel(double* const* __restrict__ panels, int n, int k, int chunk_rows,
+            const double* __restrict__ r, double* __restrict__ c, double* partials,
+            unsigned* panel_tickets, DevState* st, int pass) {
+    if (!st->go || (pass == 2 && !st->second_pass)) return;
+    const int p = blockIdx.x, chunk = blockIdx.y, nchunks = gridDim.y;
+    const double* __restrict__ vp = panels[p];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int q = lane & 3, rsub = lane >> 2;
+    const long long row0 = (long long)chunk * chunk_rows;
+    const long long row1 = min((long long)n, row0 + chunk_rows);
+    double acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    for (long long base = row0 + warp * 8; base < row1; base += 64) {
+        const long long row = base + rsub;
+        if (row < row1) {
+            const double2* src = reinterpret_cast<const double2*>(vp + row * 32 + q * 8);
+            const double2 a0 = __ldg(src), a1 = __ldg(src + 1), a2 = __ldg(src + 2),
+                          a3 = __ldg(src + 3);
+            const double rv = __ldg(r + row);
+            acc[0] = fma(a0.x, rv, acc[0]);
+            acc[1] = fma(a0.y, rv, acc[1]);
+            acc[2] = fma(a1.x, rv, acc[2]);
+            acc[3] = fma(a1.y, rv, acc[3]);
+            acc[4] = fma(a2.x, rv, acc[4]);
+            acc[5] = fma(a2.y, rv, acc[5]);
+            acc[6] = fma(a3.x, rv, acc[6]);
+            acc[7] = fma(a3.y, rv, acc[7]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 4);
+        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 8);
+        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 16);
+    }
+    __shared__ double sm[8][32];
+    __shared__ bool last;
+    if (lane < 4) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) sm[warp][lane * 8 + i] = acc[i];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += sm[w][threadIdx.x];
+        partials[((long long)p * nchunks + chunk) * 32 + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned t = atomicAdd(&panel_tickets[p], 1u);
+        last = (t == (unsigned)nchunks - 1);
+        if (last) panel_tickets[p] = 0u;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (int ch = 0; ch < nchunks; ++ch)
+            s += partials[((long long)p * nchunks + ch) * 32 + threadIdx.x];
+        const int col = p * 32 + threadIdx.x;
+        if (col < k) {
+            c[col] = s;
+            if (!isfinite(s)) st->coeff_nonfinite = 1;
+        }
+    }
+}
+
+// out = r - V c (subtract) or out = V c; 32 rows per block, warps split the
+// panels.  Sum of squares of out reduced by the last block, then `hook`.
+__global__ void __launch_bounds__(kThreads)
+v_c_kernel(double* const* __restrict__ panels, int n, int k, const double* __restrict__ c,
+           const double* r_in, double* out, int subtract, double* partials, unsigned* ticket,
+           DevState* st, int hook, int m_rows, int guarded, int pass) {
+    if (guarded && (!st->go || (pass == 2 && !st->second_pass))) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int q = lane & 3, rsub = lane >> 2;
+    const long long row0 = (long long)blockIdx.x * 32;
+    const int P = (k + 31) / 32;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int p = warp; p < P; p += 8) {
+        const double* __restrict__ vp = panels[p];
+        double cv[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int col = p * 32 + q * 8 + i;
+            cv[i] = col < k ? c[col] : 0.0;
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const long long row = row0 + s * 8 + rsub;
+            if (row < n) {
+                const double2* src = reinterpret_cast<const double2*>(vp + row * 32 + q * 8);
+                const double2 a0 = __ldg(src), a1 = __ldg(src + 1), a2 = __ldg(src + 2),
+                              a3 = __ldg(src + 3);
+                double t = acc[s];
+                t = fma(a0.x, cv[0], t);
+                t = fma(a0.y, cv[1], t);
+                t = fma(a1.x, cv[2], t);
+                t = fma(a1.y, cv[3], t);
+                t = fma(a2.x, cv[4], t);
+                t = fma(a2.y, cv[5], t);
+                t = fma(a3.x, cv[6], t);
+                t = fma(a3.y, cv[7], t);
+                acc[s] = t;
+            }
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 1);
+        acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 2);
+    }
+    __shared__ double sm[8][32];
+    __shared__ double red[32];
+    if (q == 0) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) sm[warp][s * 8 + rsub] = acc[s];
+    }
+    __syncthreads();
+    double sq = 0.0;
+    if (threadIdx.x < 32) {
+        const long long row = row0 + threadIdx.x;
+        double y = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) y += sm[w][threadIdx.x];
+        if (row < n) {
+            const double o = subtract ? r_in[row] - y : y;
+            out[row] = o;
+            sq = o * o;
+        }
+    }
+    if (hook == kHookNone) return;
+    const double bs = block_sum(sq, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+    if (arrive_last(ticket, gridDim.x)) {
+        double a = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) a += partials[b];
+        a = block_sum(a, red);
+        if (threadIdx.x == 0) {
+            st->norm_after = sqrt(a);
+            if (hook == kHookRightPass1) {
+                const double before = st->norm_before, after = st->norm_after;
+                const bool again = isfinite(before) && isfinite(after) &&
+                                   after < 0.70710678118654757 * before;
+                st->second_pass = again ? 1 : 0;
+                if (!again) decide_right(st, m_rows, n);
+            } else {
+                decide_right(st, m_rows, n);
+            }
+        }
+    }
+}
+
+__global__ void normalize_right_kernel(const double* r, int n, double* vcol, double* vnew,
+                                       const DevState* st) {
+    if (!st->go || !st->right_rank) return;
+    const double inv = st->inv_right;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = r[i] * inv;
+        vcol[i * 32] = v;
+        vnew[i] = v;
+    }
+}
+
+// Left DGKS pass: y -= c u with reductions ||y||^2, u.y, y.b.
+__global__ void __launch_bounds__(kThreads)
+left_pass_kernel(double* y, const double* u, const double* b, int m, const RedResult* spmv_red,
+                 double* partials, unsigned* ticket, DevState* st, int pass, int n_cols,
+                 double* alpha, double* beta, double* g) {
+    if (!st->go || (pass == 2 && !st->second_pass)) return;
+    const double c = pass == 1 ? spmv_red->dot : st->pass_coeff;
+    double sq = 0.0, du = 0.0, db = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double ui = u[i];
+        const double v = y[i] - c * ui;
+        y[i] = v;
+        sq = fma(v, v, sq);
+        du = fma(v, ui, du);
+        db = fma(v, b[i], db);
+    }
+    __shared__ double red[32];
+    const double s0 = block_sum(sq, red);
+    const double s1 = block_sum(du, red);
+    const double s2 = block_sum(db, red);
+    if (threadIdx.x == 0) {
+        partials[3 * blockIdx.x] = s0;
+        partials[3 * blockIdx.x + 1] = s1;
+        partials[3 * blockIdx.x + 2] = s2;
+    }
+    if (!arrive_last(ticket, gridDim.x)) return;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (unsigned blk = threadIdx.x; blk < gridDim.x; blk += blockDim.x) {
+        a0 += partials[3 * blk];
+        a1 += partials[3 * blk + 1];
+        a2 += partials[3 * blk + 2];
+    }
+    a0 = block_sum(a0, red);
+    a1 = block_sum(a1, red);
+    a2 = block_sum(a2, red);
+    if (threadIdx.x != 0) return;
+    const double after = sqrt(a0);
+    st->b_dot = a2;
+    if (pass == 1) {
+        st->left_scale = spmv_red->nonfinite ? __builtin_nan("") : sqrt(spmv_red->sq_t);
+        st->norm_before = spmv_red->nonfinite ? __builtin_nan("") : sqrt(spmv_red->sq_out);
+        st->left_coeff = c;
+        st->left_norm = after;
+        st->pass_coeff = a1;
+        const double before = st->norm_before;
+        const bool again = isfinite(before) && isfinite(after) &&
+                           after < 0.70710678118654757 * before;
+        st->second_pass = again ? 1 : 0;
+        if (!again) decide_left(st, m, n_cols, alpha, beta, g);
+    } else {
+        st->left_coeff += c;
+        st->left_norm = after;
+        decide_left(st, m, n_cols, alpha, beta, g);
+    }
+}
+
+__global__ void normalize_left_kernel(const double* y, double* u, int m, const DevState* st) {
+    if (!st->go || !st->left_rank) return;
+    const double inv = st->inv_left;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x)
+        u[i] = y[i] * inv;
+}
+
+__global__ void scale_copy_kernel(const double* src, double* dst, long long n, double s) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i] * s;
+}
+
+// Incremental Givens QR of the lower-bidiagonal T, with sqrt(lambda) I rows
+// folded in by one extra rotation per column (the damped LSQR recurrence of
+// Paige and Saunders), then back substitution for y.  qr = [rho | theta |
+// phi | y] (4 x cap); state = [c, s, rhobar, phibar, processed, flags].
+__global__ void projected_solve_kernel(const double* alpha, const double* beta, const double* g,
+                                       int k, int rows_t, double lambda, double* qr, int cap,
+                                       double* state, double rcond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double* rho = qr;
+    double* theta = qr + cap;
+    double* phi = qr + 2 * (long long)cap;
+    double* y = qr + 3 * (long long)cap;
+    double c = state[0], s = state[1], rhobar = state[2], phibar = state[3];
+    int done = (int)state[4];
+    const double root = sqrt(lambda);
+    for (int j = done; j < k; ++j) {
+        if (j == 0) {
+            rhobar = alpha[0];
+            phibar = g[0];
+        } else {
+            // the rotation of column j-1 acting on rows (j-1, j) meets column j
+            theta[j] = s * alpha[j];
+            rhobar = c * alpha[j];
+        }
+        if (lambda > 0.0) {
+            const double r = hypot(rhobar, root);
+            const double c1 = rhobar / r;
+            phibar = c1 * phibar;
+            rhobar = r;
+        }
+        if (j + 1 < rows_t) {
+            const double b = beta[j];
+            const double r = hypot(rhobar, b);
+            c = rhobar / r;
+            s = b / r;
+            rho[j] = r;
+            phi[j] = c * phibar;
+            phibar = -s * phibar + c * g[j + 1];
+        } else {
+            rho[j] = rhobar;
+            phi[j] = phibar;
+            c = 1.0;
+            s = 0.0;
+        }
+    }
+    state[0] = c;
+    state[1] = s;
+    state[2] = rhobar;
+    state[3] = phibar;
+    state[4] = (double)k;
+    // back substitution R y = phi
+    int flags = 0;
+    double ynext = 0.0;
+    for (int j = k - 1; j >= 0; --j) {
+        double num = phi[j];
+        if (j + 1 < k) num -= theta[j + 1] * ynext;
+        if (!(rho[j] != 0.0)) flags |= 1;
+        ynext = num / rho[j];
+        y[j] = ynext;
+    }
+    // LINPACK-style estimate of ||R^{-1}|| for the rank test the reference
+    // makes with dgelsy (rcond = min(1/2, 64 eps max(rows, cols))): solve
+    // R^T z = e with e_j = +-1 chosen to grow |z|, then R w = z.
+    if (lambda == 0.0 && k > 0) {
+        double rmax = 0.0, zprev = 0.0, znorm2 = 0.0;
+        for (int j = 0; j < k; ++j) {
+            const double off = j > 0 ? theta[j] : 0.0;
+            rmax = fmax(rmax, fabs(rho[j]) + fabs(off));
+            const double t = -off * zprev;
+            const double e = t >= 0.0 ? 1.0 : -1.0;
+            const double z = (e + t) / rho[j];
+            zprev = z;
+            znorm2 += z * z;
+        }
+        // ||R^{-1}|| >= ||z|| / ||e|| with ||e|| = sqrt(k)
+        const double cond = rmax * sqrt(znorm2 / (double)k);
+        if (!(cond * rcond < 1.0)) flags |= 2;
+    }
+    state[5] = (double)flags;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ panels ----
+
+PanelStore::~PanelStore() {
+    for (double* p : host_) cudaFree(p);
+    cudaFree(table_);
+}
+
+void PanelStore::ensure_columns(int cols) {
+    const int need = (cols + 31) / 32;
+    if (need <= panels()) return;
+    while (panels() < need) {
+        double* p = nullptr;
+        AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * 32 * static_cast<size_t>(n_)));
+        AMFLS_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * 32 * static_cast<size_t>(n_), stream_));
+        host_.push_back(p);
+    }
+    if (need > table_cap_) {
+        int cap = std::max(64, table_cap_);
+        while (cap < need) cap *= 2;
+        double** t = nullptr;
+        AMFLS_CUDA(cudaMalloc(&t, sizeof(double*) * cap));
+        if (table_) {
+            AMFLS_CUDA(cudaStreamSynchronize(stream_));
+            cudaFree(table_);
+        }
+        table_ = t;
+        table_cap_ = cap;
+    }
+    AMFLS_CUDA(cudaMemcpyAsync(table_, host_.data(), sizeof(double*) * host_.size(),
+                               cudaMemcpyHostToDevice, stream_));
+    // the host vector may be reallocated by a later push_back before the copy
+    // runs, so make the copy complete now
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+// ------------------------------------------------------------ timing ----
+
+struct LevelTiming {
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<std::pair<int, int>> at_pairs, a_pairs;  // event indices
+    cudaEvent_t get() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            AMFLS_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    ~LevelTiming() {
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
+// --------------------------------------------------------- workspace ----
+
+Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regularization,
+                     int maximum_basis_size, cudaStream_t stream, bool time_operators)
+    : op_(op), stream_(stream), m_(op.rows()), n_(op.cols()), reg_(regularization),
+      time_ops_(time_operators), b_(d_b) {
+    if (m_ <= 0 || n_ <= 0) throw std::invalid_argument("block Golub-Kahan operator dimensions must be positive");
+    if (d_b == nullptr) throw std::invalid_argument("block Golub-Kahan right-hand side must not be null");
+    if (!std::isfinite(regularization) || regularization < 0.0)
+        throw std::invalid_argument("block Golub-Kahan regularization must be finite and nonnegative");
+    if (maximum_basis_size < 0) throw std::invalid_argument("block Golub-Kahan basis limit must be nonnegative");
+    const int mn = std::min(m_, n_);
+    basis_limit_ = maximum_basis_size > 0 ? std::min(maximum_basis_size, mn) : mn;
+    timing_ = std::make_unique<LevelTiming>();
+    AMFLS_CUDA(cudaMalloc(&dstate_, sizeof(DevState)));
+    AMFLS_CUDA(cudaMalloc(&red_, sizeof(RedResult) * 4));
+    // scratch: V^T r partials ((target blocks + panels) x 32), then the
+    // per-block norm partials of the V c sweep (n/32 + slack)
+    const long long max_panels = basis_limit_ / 32 + 2;
+    vc_partials_offset_ = (kGemvTargetBlocks + max_panels) * 32 + 6 * 1216;
+    const long long pcount = vc_partials_offset_ + (n_ + 31) / 32 + 1024;
+    AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * pcount));
+    const long long ncounters = 64 + max_panels + 64;
+    AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * ncounters));
+    AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * ncounters, stream_));
+    AMFLS_CUDA(cudaMalloc(&zeros_n_, sizeof(double) * n_));
+    AMFLS_CUDA(cudaMemsetAsync(zeros_n_, 0, sizeof(double) * n_, stream_));
+    AMFLS_CUDA(cudaMalloc(&R_, sizeof(double) * n_));
+    AMFLS_CUDA(cudaMalloc(&vnew_, sizeof(double) * n_));
+    AMFLS_CUDA(cudaMalloc(&Y_, sizeof(double) * m_));
+    ucap_ = 1;
+    AMFLS_CUDA(cudaMalloc(&U_, sizeof(double) * m_ * ucap_));
+    V_ = std::make_unique<PanelStore>(n_, stream_);
+    std::memset(&host_, 0, sizeof(host_));
+    host_.reliable = 1;
+    host_.basis_limit = basis_limit_;
+    AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
+}
+
+Workspace::~Workspace() {
+    cudaStreamSynchronize(stream_);
+    cudaFree(dstate_);
+    cudaFree(red_);
+    cudaFree(partials_);
+    cudaFree(counter_);
+    cudaFree(zeros_n_);
+    cudaFree(R_);
+    cudaFree(vnew_);
+    cudaFree(Y_);
+    cudaFree(U_);
+    cudaFree(P_);
+    cudaFree(c1_);
+    cudaFree(c2_);
+    cudaFree(alpha_);
+    cudaFree(beta_);
+    cudaFree(g_);
+    cudaFree(qr_);
+    cudaFree(qr_state_);
+}
+
+void Workspace::ensure_t_capacity(int cols) {
+    if (cols + 2 <= tcap_ && cols <= ccap_) return;
+    int cap = std::max(1024, tcap_);
+    while (cap < cols + 2) cap *= 2;
+    auto grow = [&](double*& p, size_t old_count, size_t new_count) {
+        double* q = nullptr;
+        AMFLS_CUDA(cudaMalloc(&q, sizeof(double) * new_count));
+        AMFLS_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * new_count, stream_));
+        if (p) {
+            AMFLS_CUDA(cudaMemcpyAsync(q, p, sizeof(double) * old_count, cudaMemcpyDeviceToDevice,
+                                       stream_));
+            AMFLS_CUDA(cudaStreamSynchronize(stream_));
+            cudaFree(p);
+        }
+        p = q;
+    };
+    const size_t old = tcap_;
+    grow(alpha_, old, cap);
+    grow(beta_, old, cap);
+    grow(g_, old, cap);
+    grow(c1_, old, cap);
+    grow(c2_, old, cap);
+    // the QR arrays are laid out by capacity: rebuild them from scratch
+    cudaFree(qr_);
+    qr_ = nullptr;
+    AMFLS_CUDA(cudaMalloc(&qr_, sizeof(double) * 4 * cap));
+    if (!qr_state_) AMFLS_CUDA(cudaMalloc(&qr_state_, sizeof(double) * 8));
+    AMFLS_CUDA(cudaMemsetAsync(qr_state_, 0, sizeof(double) * 8, stream_));
+    tcap_ = cap;
+    ccap_ = cap;
+}
+
+void Workspace::initialize(const double* d_aux, int aux_cols) {
+    if (initialized_) throw std::logic_error("block Golub-Kahan workspace is already initialized");
+    initialized_ = true;
+    // ||b|| (scaled two-pass, stands in for dnrm2)
+    NormResult* nr = nullptr;
+    AMFLS_CUDA(cudaMallocAsync(&nr, sizeof(NormResult), stream_));
+    VectorSet set{};
+    set.v[0] = b_;
+    set.n[0] = m_;
+    set.count = 1;
+    norm_passes(set, nr, partials_, counter_ + 1, stream_);
+    NormResult h{};
+    AMFLS_CUDA(cudaMemcpyAsync(&h, nr, sizeof(NormResult), cudaMemcpyDeviceToHost, stream_));
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    AMFLS_CUDA(cudaFreeAsync(nr, stream_));
+    if (h.nonfinite[0]) throw std::invalid_argument("block Golub-Kahan right-hand side must be finite");
+    b_norm_ = euclid_from(h, 0);
+    ensure_t_capacity(64);
+    if (std::isfinite(b_norm_) && b_norm_ > 0.0 && basis_limit_ > 0) {
+        const double inv = 1.0 / b_norm_;
+        scale_copy_kernel<<<std::max<long long>(1, std::min<long long>(1216, (m_ + 255) / 256)), 256, 0,
+                            stream_>>>(b_, U_, m_, inv);
+        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_CUDA(cudaMemcpyAsync(g_, &b_norm_, sizeof(double), cudaMemcpyHostToDevice, stream_));
+        host_.left_width = 1;
+        host_.rows_t = 1;
+        host_.active_first = 0;
+    }
+    std::memset(&host_.audit, 0, sizeof(host_.audit));
+    AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
+    host_expected_k_ = host_.k;
+    host_expected_depth_ = host_.depth;
+    if (b_norm_ > 0.0 && aux_cols > 0) append_left_seed(d_aux, aux_cols);
+}
+
+int Workspace::append_left_seed(const double* d_seed, int cols) {
+    (void)d_seed;
+    if (cols <= 0) return 0;
+    throw std::runtime_error("block (width > 1) levels are not available in this build");
+}
+
+bool Workspace::block_level() {
+    throw std::runtime_error("block (width > 1) levels are not available in this build");
+}
+
+void Workspace::enqueue_width_one_level() {
+    const int k = host_expected_k_;
+    ensure_t_capacity(k + 2);
+    V_->ensure_columns(k + 1);
+    // timing events around the two operator calls
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+    level_begin_kernel<<<1, 32, 0, stream_>>>(dstate_, host_expected_depth_ + 1);
+    AMFLS_CUDA(cudaGetLastError());
+    // A^T u - beta v_prev
+    Epilogue ep;
+    ep.out = R_;
+    ep.sub = k > 0 ? V_->column(k - 1) : zeros_n_;
+    ep.sub_stride = k > 0 ? 32 : 1;
+    ep.coef = &dstate_->coupling_eff;
+    ep.red = &red_[0];
+    ep.guard = &dstate_->go;
+    ep.partials = partials_;
+    ep.counter = counter_ + 2;
+    if (time_ops_) {
+        e0 = timing_->get();
+        AMFLS_CUDA(cudaEventRecord(e0, stream_));
+    }
+    if (!op_.product1(true, U_, ep, stream_)) {
+        throw std::runtime_error("operator has no fused device product");
+    }
+    if (time_ops_) {
+        e1 = timing_->get();
+        AMFLS_CUDA(cudaEventRecord(e1, stream_));
+        timing_->at_pairs.emplace_back((int)(timing_->used - 2), (int)(timing_->used - 1));
+    }
+    right_scales_kernel<<<1, 32, 0, stream_>>>(dstate_, &red_[0], m_, n_, k == 0 ? 1 : 0);
+    AMFLS_CUDA(cudaGetLastError());
+    if (k > 0) {
+        const int P = (k + 31) / 32;
+        const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
+        const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + P - 1) / P));
+        const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
+        const dim3 tgrid(P, chunks);
+        const int ngrid = (int)((n_ + 31) / 32);
+        for (int pass = 1; pass <= 2; ++pass) {
+            double* c = pass == 1 ? c1_ : c2_;
+            vt_r_kernel<<<tgrid, kThreads, 0, stream_>>>(V_->device_table(), n_, k, chunk_rows, R_,
+                                                         c, partials_, counter_ + 64, dstate_, pass);
+            AMFLS_CUDA(cudaGetLastError());
+            v_c_kernel<<<ngrid, kThreads, 0, stream_>>>(
+                V_->device_table(), n_, k, c, R_, R_, 1, partials_ + vc_partials_offset_,
+                counter_ + 3, dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, 1, pass);
+            AMFLS_CUDA(cudaGetLastError());
+        }
+    }
+    normalize_right_kernel<<<(int)std::min<long long>(1216, (n_ + 255) / 256), 256, 0, stream_>>>(
+        R_, n_, V_->column(k), vnew_, dstate_);
+    AMFLS_CUDA(cudaGetLastError());
+    // y = A v - ||r|| u, with ||A v||, ||y||, u.y
+    Epilogue el;
+    el.out = Y_;
+    el.sub = U_;
+    el.sub_stride = 1;
+    el.coef = &dstate_->right_factor;
+    el.dot_vec = U_;
+    el.red = &red_[1];
+    el.guard = &dstate_->go;
+    el.partials = partials_;
+    el.counter = counter_ + 2;
+    if (time_ops_) {
+        e2 = timing_->get();
+        AMFLS_CUDA(cudaEventRecord(e2, stream_));
+    }
+    op_.product1(false, vnew_, el, stream_);
+    if (time_ops_) {
+        e3 = timing_->get();
+        AMFLS_CUDA(cudaEventRecord(e3, stream_));
+        timing_->a_pairs.emplace_back((int)(timing_->used - 2), (int)(timing_->used - 1));
+    }
+    (void)e0; (void)e1; (void)e2; (void)e3;
+    const int lgrid = (int)std::max<long long>(1, std::min<long long>(1216, (m_ + 1023) / 1024));
+    for (int pass = 1; pass <= 2; ++pass) {
+        left_pass_kernel<<<lgrid, kThreads, 0, stream_>>>(Y_, U_, b_, m_, &red_[1], partials_,
+                                                          counter_ + 4, dstate_, pass, n_, alpha_,
+                                                          beta_, g_);
+        AMFLS_CUDA(cudaGetLastError());
+    }
+    normalize_left_kernel<<<(int)std::min<long long>(1216, (m_ + 255) / 256), 256, 0, stream_>>>(
+        Y_, U_, m_, dstate_);
+    AMFLS_CUDA(cudaGetLastError());
+    host_expected_k_ += 1;
+    host_expected_depth_ += 1;
+}
+
+void Workspace::advance_to(int target_depth) {
+    if (!initialized_) throw std::logic_error("block Golub-Kahan workspace is not initialized");
+    if (host_.left_width + host_.pending > 1) {
+        while (can_advance() && host_.depth < target_depth) {
+            if (!block_level()) break;
+        }
+        return;
+    }
+    host_expected_k_ = host_.k;
+    host_expected_depth_ = host_.depth;
+    int levels = target_depth - host_.depth;
+    levels = std::min(levels, basis_limit_ - host_.k);
+    if (levels <= 0) return;
+    // all allocations for the run happen before the first launch, so the
+    // enqueue loop never waits for the device
+    ensure_t_capacity(host_.k + levels + 2);
+    V_->ensure_columns(host_.k + levels + 1);
+    for (int i = 0; i < levels; ++i) enqueue_width_one_level();
+}
+
+bool Workspace::advance_level() {
+    const int before = host_.depth;
+    advance_to(host_.depth + 1);
+    sync();
+    return host_.depth > before && host_.level_ok;
+}
+
+void Workspace::sync() {
+    AMFLS_CUDA(cudaMemcpyAsync(&host_, dstate_, sizeof(DevState), cudaMemcpyDeviceToHost, stream_));
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Workspace::take_operator_seconds(double& a_seconds, double& at_seconds) {
+    a_seconds = 0.0;
+    at_seconds = 0.0;
+    if (!time_ops_) {
+        timing_->used = 0;
+        return;
+    }
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    auto sum = [&](std::vector<std::pair<int, int>>& pairs) {
+        double t = 0.0;
+        for (auto& p : pairs) {
+            float ms = 0.0f;
+            AMFLS_CUDA(cudaEventElapsedTime(&ms, timing_->pool[p.first], timing_->pool[p.second]));
+            t += ms * 1e-3;
+        }
+        pairs.clear();
+        return t;
+    };
+    at_seconds = sum(timing_->at_pairs);
+    a_seconds = sum(timing_->a_pairs);
+    timing_->used = 0;
+}
+
+void Workspace::solve_projected(double* d_x) {
+    const int k = host_.k;
+    projected_flags_ = 0;
+    if (k == 0) {
+        AMFLS_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n_, stream_));
+        return;
+    }
+    const double rcond = std::min(0.5, 64.0 * kEps * std::max(host_.rows_t, k));
+    projected_solve_kernel<<<1, 32, 0, stream_>>>(alpha_, beta_, g_, k, host_.rows_t, reg_, qr_,
+                                                  tcap_, qr_state_, rcond);
+    AMFLS_CUDA(cudaGetLastError());
+    const double* y = qr_ + 3 * (long long)tcap_;
+    v_c_kernel<<<(int)((n_ + 31) / 32), kThreads, 0, stream_>>>(
+        V_->device_table(), n_, k, y, nullptr, d_x, 0, partials_, counter_ + 5, dstate_, kHookNone,
+        m_, 0, 1);
+    AMFLS_CUDA(cudaGetLastError());
+    double st[8];
+    AMFLS_CUDA(cudaMemcpyAsync(st, qr_state_, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream_));
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    projected_flags_ = (int)st[5];
+}
+
+}  // namespace amfls_gpu

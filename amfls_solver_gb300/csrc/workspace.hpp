@@ -1,0 +1,146 @@
+// Block Golub-Kahan workspace on the device.
+//
+// GB300 restatement of BlockGolubKahanWorkspace
+// (src/algorithms/mathematics/krylov/krylov_workspace.hpp:93-189 and
+// krylov_workspace.cpp:335-963).  Data layout in HBM:
+//   V  right basis, n x k FP64, stored as panels of 32 columns; panel p is a
+//      row-major n x 32 tile (row i of the panel = 256 contiguous bytes), so a
+//      sweep over V reads contiguous 2 KB runs and a new column is one
+//      strided write.  Panels are allocated on demand and never moved.
+//   U  active left block, m x w column-major (only the unconsumed frontier,
+//      as in the reference); P pending P*Omega, m x p.
+//   T  projected operator: lower bidiagonal at width one, kept as the two
+//      diagonals alpha_j = T(j, j), beta_{j+1} = T(j+1, j); g = U^T b.
+// Width-one levels run entirely on the device (DevState decisions); wider
+// blocks use the host-synchronised block path.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "device_operator.hpp"
+#include "workspace_state.hpp"
+
+namespace amfls_gpu {
+
+
+class PanelStore {
+public:
+    PanelStore(int n, cudaStream_t stream) : n_(n), stream_(stream) {}
+    ~PanelStore();
+    void ensure_columns(int cols);  // allocate (zeroed) panels to hold `cols` columns
+    double* column(int j) const { return host_[j / 32] + (j % 32); }  // stride 32
+    double* const* device_table() const { return table_; }
+    int panels() const { return static_cast<int>(host_.size()); }
+    int n() const { return n_; }
+    size_t bytes() const { return host_.size() * static_cast<size_t>(n_) * 32 * sizeof(double); }
+
+private:
+    int n_;
+    cudaStream_t stream_;
+    std::vector<double*> host_;
+    double** table_ = nullptr;
+    int table_cap_ = 0;
+};
+
+struct LevelTiming;  // events around operator calls
+
+class Workspace {
+public:
+    Workspace(const DeviceOperator& op, const double* d_b, double regularization,
+              int maximum_basis_size, cudaStream_t stream, bool time_operators);
+    ~Workspace();
+    Workspace(const Workspace&) = delete;
+    Workspace& operator=(const Workspace&) = delete;
+
+    // krylov_workspace.cpp:470-503; the auxiliary block (m x cols, device,
+    // column-major) may be null when cols == 0.
+    void initialize(const double* d_aux, int aux_cols);
+    // krylov_workspace.cpp:505-587
+    int append_left_seed(const double* d_seed, int cols);
+    // Enqueue levels until `target_depth` or until the process cannot
+    // advance; no host synchronisation at width one.
+    void advance_to(int target_depth);
+    // One level, synchronised (widening trials).
+    bool advance_level();
+    // Copy the device state back (a synchronisation point).
+    void sync();
+
+    int depth() const { return host_.depth; }
+    int basis_rank() const { return host_.k; }
+    int basis_limit() const { return basis_limit_; }
+    int active_left_width() const { return host_.left_width; }
+    bool can_advance() const {
+        return initialized_ && host_.reliable && host_.left_width + host_.pending > 0 &&
+               host_.k < basis_limit_;
+    }
+    double right_hand_side_norm() const { return b_norm_; }
+    const StepAudit& last_step_audit() const { return host_.audit; }
+    const DevState& state() const { return host_; }
+
+    // Projected solve (krylov_workspace.cpp:833-909): writes the candidate
+    // x = V y into d_x (n).  Returns false when the projected problem was
+    // flagged as numerically rank deficient (see projected_flags()).
+    void solve_projected(double* d_x);
+    int projected_flags() const { return projected_flags_; }
+
+    // accumulated device timings of search operator calls since the last call
+    void take_operator_seconds(double& a_seconds, double& at_seconds);
+
+    const DeviceOperator& op() const { return op_; }
+    const double* b() const { return b_; }
+    cudaStream_t stream() const { return stream_; }
+    double* scratch_partials() const { return partials_; }
+    unsigned* scratch_counter() const { return counter_; }
+
+private:
+    void enqueue_width_one_level();
+    bool block_level();
+    void ensure_t_capacity(int cols);
+
+    const DeviceOperator& op_;
+    cudaStream_t stream_;
+    int m_, n_;
+    double reg_;
+    int basis_limit_;
+    bool initialized_ = false;
+    bool time_ops_;
+    const double* b_;   // caller's device b (kept alive by the caller)
+    double b_norm_ = 0.0;
+
+    DevState host_{};
+    DevState* dstate_ = nullptr;
+    RedResult* red_ = nullptr;  // [4] reduction slots
+    double* partials_ = nullptr;
+    long long vc_partials_offset_ = 0;
+    unsigned* counter_ = nullptr;   // self-resetting tickets: misc + one per V panel
+    double* zeros_n_ = nullptr;
+
+    std::unique_ptr<PanelStore> V_;
+    double* U_ = nullptr;      // m x ucap
+    int ucap_ = 0;
+    double* P_ = nullptr;      // m x pcap (pending seed)
+    int pcap_ = 0;
+    double* R_ = nullptr;      // n residual
+    double* vnew_ = nullptr;   // n
+    double* Y_ = nullptr;      // m residual
+    double* c1_ = nullptr;     // coefficients (k cap)
+    double* c2_ = nullptr;
+    int ccap_ = 0;
+    // projected operator at width one
+    double* alpha_ = nullptr;  // T(j,j)
+    double* beta_ = nullptr;   // T(j+1,j)
+    double* g_ = nullptr;      // g
+    int tcap_ = 0;
+    // incremental Givens QR of [T; sqrt(lambda) I]
+    double* qr_ = nullptr;     // rho, theta, phi (3 x tcap) + y (tcap)
+    double* qr_state_ = nullptr;  // [c, s, rhobar, phibar, processed]
+    int projected_flags_ = 0;
+    int host_expected_k_ = 0;  // k the host expects at the next enqueued level
+    int host_expected_depth_ = 0;
+    std::unique_ptr<LevelTiming> timing_;
+};
+
+}  // namespace amfls_gpu

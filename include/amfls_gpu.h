@@ -1,0 +1,148 @@
+/* amfls_gpu.h - C ABI of the GB300-native AMFLS least-squares solver.
+ *
+ * Drop-in boundary for the reference's AMFLS hot path
+ * (doloMing/amfls_solver).  Every entry point takes plain pointers and sizes;
+ * matrix and vector arguments named d_* are CUDA device pointers, `stream` is
+ * a cudaStream_t passed as void* (NULL = the legacy default stream).  All
+ * functions return AMFLS_GPU_OK (0) or an error code; amfls_gpu_last_error()
+ * gives the message of the calling thread's last failure.  Numerical outcomes
+ * are never errors: they are reported through status / stop_reason with the
+ * reference's integer values.
+ *
+ * Reference interfaces replaced (paths relative to the reference repository):
+ *   MatrixOperator contract ......... include/amfls/matrix_operator.hpp:29-89
+ *   SparseCsrOperator ............... src/algorithms/mathematics/operators/sparse_csr_operator.hpp:13-58
+ *   AmflsOptions / solve_amfls ...... include/amfls/amfls.hpp:10-25
+ *   FixedRbgkOptions / solve_fixed_rbgk include/amfls/fixed_rbgk.hpp:8-25
+ *   LeastSquaresResult / statuses ... include/amfls/least_squares_result.hpp:8-229
+ *   result tensor layout ............ bindings/torch/result_tensors.hpp:12-156
+ */
+#ifndef AMFLS_GPU_H
+#define AMFLS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    AMFLS_GPU_OK = 0,
+    AMFLS_GPU_INVALID_ARGUMENT = 1, /* std::invalid_argument in the reference */
+    AMFLS_GPU_LENGTH_ERROR = 2,     /* std::length_error / overflow_error */
+    AMFLS_GPU_LOGIC_ERROR = 3,      /* std::logic_error */
+    AMFLS_GPU_CUDA_ERROR = 4,       /* a CUDA runtime call failed */
+    AMFLS_GPU_RUNTIME_ERROR = 5     /* any other failure */
+};
+
+/* SolverStatus (least_squares_result.hpp:8-14) */
+enum {
+    AMFLS_STATUS_SUCCESS = 0,
+    AMFLS_STATUS_WORK_LIMIT = 1,
+    AMFLS_STATUS_BASIS_LIMIT = 2,
+    AMFLS_STATUS_PRECISION_LIMIT = 3,
+    AMFLS_STATUS_NUMERICAL_BREAKDOWN = 4
+};
+
+/* Widths of the packed result arrays (result_tensors.hpp:12-16). */
+#define AMFLS_GPU_METRICS 21
+#define AMFLS_GPU_COUNTERS 36
+#define AMFLS_GPU_TIMINGS 9
+#define AMFLS_GPU_TRACE_FLOAT 29
+#define AMFLS_GPU_TRACE_INT 4
+
+typedef struct amfls_gpu_operator amfls_gpu_operator;
+
+/* MatrixOperatorValidationErrorModel (matrix_operator.hpp:21-27). */
+typedef struct {
+    double operator_norm_upper_bound;
+    double operator_norm_lower_bound;
+    long long apply_rounding_steps;
+    long long apply_transpose_rounding_steps;
+} amfls_gpu_validation_error_model;
+
+/* AmflsOptions (amfls.hpp:10-20) and FixedRbgkOptions (fixed_rbgk.hpp:8-18). */
+typedef struct {
+    double regularization;       /* lambda >= 0 */
+    double tolerance;            /* (0, 1) */
+    double failure_probability;  /* (0, 1); validated, does not change the algorithm */
+    int maximum_epochs;          /* 0 = default */
+    int maximum_basis_size;      /* 0 = min(rows, cols) */
+    uint64_t seed;
+    uint64_t stream;             /* random stream id (not a CUDA stream) */
+    int maximum_depth;           /* 0 = min(rows, cols); fixed RBGK: required > 0 */
+    int maximum_auxiliary_width; /* 0 = default */
+    int auxiliary_width;         /* fixed RBGK only */
+    int stop_early;              /* fixed RBGK only */
+    int time_operators;          /* record CUDA-event times of operator calls (default 1) */
+} amfls_gpu_options;
+
+/* LeastSquaresResult, packed like the torch binding's tensors. */
+typedef struct {
+    int rows, cols, iterations, depth, auxiliary_width, basis_rank;
+    int status, stop_reason;
+    double metrics[AMFLS_GPU_METRICS];
+    long long counters[AMFLS_GPU_COUNTERS];
+    double timings[AMFLS_GPU_TIMINGS];
+    int trace_rows; /* checkpoints evaluated; rows beyond the capacity are dropped */
+} amfls_gpu_result;
+
+/* Sets the reference's defaults (amfls.hpp:10-20; fixed_rbgk.hpp:8-18). */
+void amfls_gpu_default_options(amfls_gpu_options* options);
+
+/* Message of the calling thread's last error ("" if none). */
+const char* amfls_gpu_last_error(void);
+
+/* Replaces SparseCsrOperator's constructor (sparse_csr_operator.cpp:14-130):
+ * validates the CSR arrays (int64 offsets and indices, FP64 values, device
+ * memory), copies them, builds the transpose and the certified norm model.
+ * The caller may free its arrays afterwards. */
+int amfls_gpu_csr_operator_create(int rows, int cols, const int64_t* d_row_offsets,
+                                  const int64_t* d_column_indices, const double* d_values,
+                                  int64_t nonzeros, void* stream, amfls_gpu_operator** out);
+
+/* Dense operator over caller-owned device memory (not copied; keep it alive):
+ * column_major = 0 is the row-major layout of RowMajorDenseOperator
+ * (row_major_dense_operator.cpp), 1 the column-major DenseOperator
+ * (dense_operator.cpp). */
+int amfls_gpu_dense_operator_create(int rows, int cols, const double* d_values, int column_major,
+                                    void* stream, amfls_gpu_operator** out);
+
+int amfls_gpu_operator_destroy(amfls_gpu_operator* op);
+int amfls_gpu_operator_rows(const amfls_gpu_operator* op);
+int amfls_gpu_operator_cols(const amfls_gpu_operator* op);
+
+/* MatrixOperator::apply / apply_transpose (matrix_operator.hpp:36-44):
+ * column-major device blocks X (cols x block_cols), Y (rows x block_cols). */
+int amfls_gpu_operator_apply(const amfls_gpu_operator* op, const double* d_x, int block_cols,
+                             double* d_y, void* stream);
+int amfls_gpu_operator_apply_transpose(const amfls_gpu_operator* op, const double* d_y,
+                                       int block_cols, double* d_x, void* stream);
+
+/* MatrixOperator::relative_block_product_cost (matrix_operator.hpp:50-55). */
+double amfls_gpu_operator_relative_block_product_cost(const amfls_gpu_operator* op,
+                                                      int block_cols);
+
+/* MatrixOperator::validation_error_model (matrix_operator.hpp:57-60). */
+int amfls_gpu_operator_validation_error_model(const amfls_gpu_operator* op,
+                                              amfls_gpu_validation_error_model* out);
+
+/* solve_amfls (amfls.hpp:22-25): d_b (rows) and d_solution (cols) are device
+ * vectors; trace_float (capacity x 29) and trace_int (capacity x 4) are host
+ * buffers (may be NULL when trace_capacity is 0). Synchronous on `stream`. */
+int amfls_gpu_solve_amfls(const amfls_gpu_operator* op, const double* d_b,
+                          const amfls_gpu_options* options, double* d_solution,
+                          amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                          int trace_capacity, void* stream);
+
+/* solve_fixed_rbgk (fixed_rbgk.hpp:22-25), same conventions. */
+int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
+                               const amfls_gpu_options* options, double* d_solution,
+                               amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                               int trace_capacity, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AMFLS_GPU_H */

@@ -1,0 +1,71 @@
+"""Host-side checks of the native library that need no GPU.
+
+The C-ABI library must load and export every entry point include/amfls_gpu.h
+declares; argument errors that are caught before any CUDA call must come back
+as error codes with a message.  No compute call is made here.
+"""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from amfls_solver_gb300 import _native
+from amfls_solver_gb300.build import LIB
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "amfls_gpu.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(amfls_gpu_[a-z_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not LIB.exists():
+        from amfls_solver_gb300 import build
+        build.build()
+    return _native.load()
+
+
+def test_header_declares_the_exported_list():
+    assert declared_functions() == sorted(_native.EXPORTED)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_default_options_match_reference_defaults(lib):
+    o = _native.default_options()
+    assert o.regularization == 0.0
+    assert o.tolerance == 1e-8
+    assert o.failure_probability == 1e-6
+    assert (o.maximum_epochs, o.maximum_depth, o.maximum_auxiliary_width,
+            o.maximum_basis_size) == (0, 0, 0, 0)
+    assert (o.seed, o.stream) == (0, 0)
+    assert o.auxiliary_width == 4 and o.stop_early == 1
+
+
+def test_null_arguments_are_errors_not_crashes(lib):
+    res = _native.Result()
+    o = _native.default_options()
+    rc = lib.amfls_gpu_solve_amfls(None, None, ctypes.byref(o), None, ctypes.byref(res), None,
+                                   None, 0, None)
+    assert rc == 1
+    assert b"solution must not be null" in lib.amfls_gpu_last_error()
+    assert lib.amfls_gpu_operator_rows(None) == -1
+    assert lib.amfls_gpu_operator_cols(None) == -1
+    handle = ctypes.c_void_p()
+    rc = lib.amfls_gpu_csr_operator_create(0, 5, None, None, None, 0, None, ctypes.byref(handle))
+    assert rc == 1 and handle.value is None
+    assert b"dimensions are invalid" in lib.amfls_gpu_last_error()
+
+
+def test_status_constants_match_reference():
+    text = HEADER.read_text()
+    for name, value in [("SUCCESS", 0), ("WORK_LIMIT", 1), ("BASIS_LIMIT", 2),
+                        ("PRECISION_LIMIT", 3), ("NUMERICAL_BREAKDOWN", 4)]:
+        assert re.search(rf"AMFLS_STATUS_{name} = {value}\b", text)
