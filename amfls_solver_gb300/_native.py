@@ -22,7 +22,8 @@ class Options(ctypes.Structure):
                 ("maximum_basis_size", ctypes.c_int), ("seed", ctypes.c_uint64),
                 ("stream", ctypes.c_uint64), ("maximum_depth", ctypes.c_int),
                 ("maximum_auxiliary_width", ctypes.c_int), ("auxiliary_width", ctypes.c_int),
-                ("stop_early", ctypes.c_int), ("time_operators", ctypes.c_int)]
+                ("stop_early", ctypes.c_int), ("time_operators", ctypes.c_int),
+                ("use_graphs", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -99,6 +100,10 @@ def check(rc: int) -> None:
 
 
 def default_options() -> Options:
+    """Reference defaults; AMFLS_GB300_USE_GRAPHS=0 in the environment turns the
+    per-interval CUDA graph off (same kernels, launched one by one)."""
     o = Options()
     load().amfls_gpu_default_options(ctypes.byref(o))
+    if os.environ.get("AMFLS_GB300_USE_GRAPHS", "1") == "0":
+        o.use_graphs = 0
     return o

@@ -67,6 +67,7 @@ amfls_gpu::SolveOptions to_options(const amfls_gpu_options* o) {
     s.auxiliary_width = o->auxiliary_width;
     s.stop_early = o->stop_early != 0;
     s.time_operators = o->time_operators != 0;
+    s.use_graphs = o->use_graphs != 0;
     return s;
 }
 
@@ -112,6 +113,7 @@ void amfls_gpu_default_options(amfls_gpu_options* o) {
     o->maximum_depth = 0;
     o->stop_early = 1;
     o->time_operators = 1;
+    o->use_graphs = 1;
 }
 
 const char* amfls_gpu_last_error(void) { return g_last_error.c_str(); }

@@ -544,7 +544,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
     const double reg = o.regularization, tol = o.tolerance;
     const auto t_start = Clock::now();
     Statistics stats;
-    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators);
+    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators, o.use_graphs);
     Evaluator ev(ws, op, d_b, reg, stats, stream);
     long long seen[4] = {0, 0, 0, 0};
     auto absorb = [&] {
@@ -822,7 +822,7 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
     const double reg = o.regularization, tol = o.tolerance;
     const auto t_start = Clock::now();
     Statistics stats;
-    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators);
+    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators, o.use_graphs);
     Evaluator ev(ws, op, d_b, reg, stats, stream);
     long long seen[4] = {0, 0, 0, 0};
     auto absorb = [&] {

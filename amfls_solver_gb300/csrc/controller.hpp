@@ -24,6 +24,7 @@ struct SolveOptions {
     int auxiliary_width = 4;  // fixed RBGK only
     bool stop_early = true;   // fixed RBGK only
     bool time_operators = true;
+    bool use_graphs = true;
 };
 
 // RunStatistics (include/amfls/least_squares_result.hpp:57-109).

@@ -222,6 +222,14 @@ int grid_1d(long long items) {
     return (int)std::max<long long>(1, std::min<long long>(kTargetBlocks, (items + 255) / 256));
 }
 
+// chunking of the long dimension for the across-contiguous product
+void split_chunks(int out_n, int in_n, int& chunks, int& chunk) {
+    const int oblocks = (out_n + 255) / 256;
+    chunks = std::max(1, std::min((kTargetBlocks + oblocks - 1) / oblocks, (in_n + 63) / 64));
+    chunk = (in_n + chunks - 1) / chunks;
+    chunks = (in_n + chunk - 1) / chunk;
+}
+
 }  // namespace
 
 void run_epilogue(const double* t, long long n, const Epilogue& ep, double* partials,
@@ -241,6 +249,16 @@ DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool co
     AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * 8));
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * 8, stream));
     AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows, cols)));
+    // partial sums of the across-contiguous product, sized once so that
+    // products can be captured into CUDA graphs
+    {
+        const int out_n = column_major ? rows : cols;  // the non-dot direction
+        const int in_n = column_major ? cols : rows;
+        int chunks = 0, chunk = 0;
+        split_chunks(out_n, in_n, chunks, chunk);
+        partial_cap_ = (long long)chunks * out_n;
+        AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * std::max<long long>(1, partial_cap_)));
+    }
     // w: acc[5] | frob(inner) | model[2] | frob(outer) | partials (inner) | partials (outer)
     double* w = nullptr;
     const int ig = grid_1d(inner), og = grid_1d(outer);
@@ -285,18 +303,11 @@ void DenseOperator::product(bool transpose, const double* x, double* y, const in
         const int grid = (int)std::max<long long>(1, std::min<long long>(kTargetBlocks * 2, (warps + 7) / 8));
         dot_rows_kernel<<<grid, kThreads, 0, s>>>(a_, ld, out_n, in_n, x, y, guard);
     } else {
+        int chunks = 0, chunk = 0;
+        split_chunks(out_n, in_n, chunks, chunk);
         const int oblocks = (out_n + 255) / 256;
-        int chunks = std::max(1, std::min((kTargetBlocks + oblocks - 1) / oblocks, (in_n + 63) / 64));
-        const int chunk = (in_n + chunks - 1) / chunks;
-        chunks = (in_n + chunk - 1) / chunk;
-        const long long need = (long long)chunks * out_n;
-        if (need > partial_cap_) {
-            auto* self = const_cast<DenseOperator*>(this);
-            AMFLS_CUDA(cudaStreamSynchronize(s));
-            cudaFree(self->partials_);
-            AMFLS_CUDA(cudaMalloc(&self->partials_, sizeof(double) * need));
-            self->partial_cap_ = need;
-        }
+        if ((long long)chunks * out_n > partial_cap_)
+            throw std::logic_error("dense operator partial buffer is too small");
         sum_cols_kernel<<<dim3(oblocks, chunks), kThreads, 0, s>>>(a_, ld, out_n, in_n, chunk, x,
                                                                    partials_, guard);
         add_chunks_kernel<<<grid_1d(out_n), kThreads, 0, s>>>(partials_, chunks, out_n, y, guard);

@@ -42,6 +42,7 @@ struct RedResult {
 
 // t_i is the i-th entry of the product.  Then
 //   out_i = t_i - (*coef) * sub[i * sub_stride]         if sub != nullptr
+//   out_i = t_i - (*coef) * panel(*sub_col)[i]           if sub_table != nullptr
 //   out_i = fma(lambda, fma_vec[i], t_i)                 if fma_vec != nullptr
 //   out_i = t_i - minus_vec[i]                           if minus_vec != nullptr
 //   out_i = t_i                                          otherwise
@@ -50,6 +51,10 @@ struct Epilogue {
     double* out = nullptr;
     const double* sub = nullptr;
     long long sub_stride = 1;
+    // alternatively the subtracted vector is column *sub_col of a table of
+    // row-major 32-column panels (read on the device at run time)
+    double* const* sub_table = nullptr;
+    const int* sub_col = nullptr;
     const double* coef = nullptr;
     const double* fma_vec = nullptr;
     double lambda = 0.0;

@@ -10,7 +10,10 @@ __device__ __forceinline__ void epilogue_row(const Epilogue& ep, int row, double
                                              double& sq_out, double& dot, double& mx_t,
                                              double& mx_out, int& nonfin) {
     double out = t;
-    if (ep.sub) out = t - (*ep.coef) * ep.sub[(long long)row * ep.sub_stride];
+    if (ep.sub_table) {
+        const int c = *ep.sub_col;
+        out = t - (*ep.coef) * ep.sub_table[c >> 5][(long long)row * 32 + (c & 31)];
+    } else if (ep.sub) out = t - (*ep.coef) * ep.sub[(long long)row * ep.sub_stride];
     else if (ep.fma_vec) out = fma(ep.lambda, ep.fma_vec[row], t);
     else if (ep.minus_vec) out = t - ep.minus_vec[row];
     if (ep.t_out) ep.t_out[row] = t;

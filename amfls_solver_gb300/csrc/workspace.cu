@@ -157,12 +157,31 @@ __device__ void decide_left(DevState* st, int m, int n, double* alpha, double* b
     if (!rank) st->go = 0;  // nothing to normalise; the process stops here
 }
 
-__global__ void level_begin_kernel(DevState* st, int target_depth) {
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool can_advance_dev(const DevState* st) {
+    return st->reliable && (st->left_width + st->pending > 0) && st->k < st->basis_limit &&
+           st->depth < st->target_depth;
+}
+
+__global__ void set_target_kernel(DevState* st, int target_depth, int iterations) {
     if (threadIdx.x != 0) return;
-    const bool go = st->reliable && (st->left_width + st->pending > 0) &&
-                    st->k < st->basis_limit && st->depth < target_depth;
+    st->target_depth = target_depth;
+    st->iterations_left = iterations;
+}
+
+__global__ void level_begin_kernel(DevState* st) {
+    if (threadIdx.x != 0) return;
+    const bool go = can_advance_dev(st) && st->iterations_left > 0;
+    st->iterations_left -= 1;
     st->go = go ? 1 : 0;
     if (!go) return;
+    st->sub_col = st->prev_right_width > 0 ? st->prev_right_first : 0;
+    st->t_mark = global_ns();
     StepAudit a;
     memset(&a, 0, sizeof(a));
     a.left_input_width = st->left_width + st->pending;
@@ -180,9 +199,10 @@ __global__ void level_begin_kernel(DevState* st, int target_depth) {
 }
 
 // after A^T u: scale and norm_before from the fused reduction
-__global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, int n,
-                                    int no_projection) {
+__global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, int n) {
     if (threadIdx.x != 0 || !st->go) return;
+    st->at_ns += global_ns() - st->t_mark;
+    const bool no_projection = st->k == 0;
     st->right_scale = red->nonfinite ? __builtin_nan("") : sqrt(red->sq_t);
     st->norm_before = red->nonfinite ? __builtin_nan("") : sqrt(red->sq_out);
     if (no_projection) {  // empty basis: no pass, the norm is the block's norm
@@ -193,11 +213,13 @@ __global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, i
 
 // c = V^T r, masked to k columns.  grid (panels, chunks); partials [P][C][32].
 __global__ void __launch_bounds__(kThreads)
-vt_r_kernel(double* const* __restrict__ panels, int n, int k, int chunk_rows,
+vt_r_kernel(double* const* __restrict__ panels, int n, int chunk_rows,
             const double* __restrict__ r, double* __restrict__ c, double* partials,
             unsigned* panel_tickets, DevState* st, int pass) {
     if (!st->go || (pass == 2 && !st->second_pass)) return;
+    const int k = st->k;  // k == 0: no projection (decided in right_scales_kernel)
     const int p = blockIdx.x, chunk = blockIdx.y, nchunks = gridDim.y;
+    if (p * 32 >= k) return;  // panel beyond the current basis
     const double* __restrict__ vp = panels[p];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int q = lane & 3, rsub = lane >> 2;
@@ -267,10 +289,11 @@ vt_r_kernel(double* const* __restrict__ panels, int n, int k, int chunk_rows,
 // out = r - V c (subtract) or out = V c; 32 rows per block, warps split the
 // panels.  Sum of squares of out reduced by the last block, then `hook`.
 __global__ void __launch_bounds__(kThreads)
-v_c_kernel(double* const* __restrict__ panels, int n, int k, const double* __restrict__ c,
+v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* __restrict__ c,
            const double* r_in, double* out, int subtract, double* partials, unsigned* ticket,
            DevState* st, int hook, int m_rows, int guarded, int pass) {
-    if (guarded && (!st->go || (pass == 2 && !st->second_pass))) return;
+    if (guarded && (!st->go || (pass == 2 && !st->second_pass) || st->k == 0)) return;
+    const int k = k_arg >= 0 ? k_arg : st->k;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int q = lane & 3, rsub = lane >> 2;
     const long long row0 = (long long)blockIdx.x * 32;
@@ -350,10 +373,13 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k, const double* __res
     }
 }
 
-__global__ void normalize_right_kernel(const double* r, int n, double* vcol, double* vnew,
-                                       const DevState* st) {
+__global__ void normalize_right_kernel(const double* r, int n, double* const* panels,
+                                       double* vnew, DevState* st) {
     if (!st->go || !st->right_rank) return;
     const double inv = st->inv_right;
+    const int k = st->k;
+    double* vcol = panels[k >> 5] + (k & 31);
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->t_mark = global_ns();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const double v = r[i] * inv;
@@ -368,6 +394,7 @@ left_pass_kernel(double* y, const double* u, const double* b, int m, const RedRe
                  double* partials, unsigned* ticket, DevState* st, int pass, int n_cols,
                  double* alpha, double* beta, double* g) {
     if (!st->go || (pass == 2 && !st->second_pass)) return;
+    if (pass == 1 && blockIdx.x == 0 && threadIdx.x == 0) st->a_ns += global_ns() - st->t_mark;
     const double c = pass == 1 ? spmv_red->dot : st->pass_coeff;
     double sq = 0.0, du = 0.0, db = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
@@ -425,6 +452,13 @@ __global__ void normalize_left_kernel(const double* y, double* u, int m, const D
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
          i += (long long)gridDim.x * blockDim.x)
         u[i] = y[i] * inv;
+}
+
+// Loop control of the captured level: continue while the next level can run.
+__global__ void level_end_kernel(DevState* st, cudaGraphConditionalHandle handle) {
+    if (threadIdx.x != 0) return;
+    const bool more = st->go && can_advance_dev(st) && st->iterations_left > 0;
+    cudaGraphSetConditional(handle, more ? 1u : 0u);
 }
 
 __global__ void scale_copy_kernel(const double* src, double* dst, long long n, double s) {
@@ -518,6 +552,14 @@ __global__ void projected_solve_kernel(const double* alpha, const double* beta, 
 
 // ------------------------------------------------------------ panels ----
 
+PanelStore::PanelStore(int n, int max_panels, cudaStream_t stream)
+    : n_(n), stream_(stream), table_cap_(std::max(1, max_panels)) {
+    // fixed-capacity device table: its address never changes, so captured
+    // kernels may keep it
+    AMFLS_CUDA(cudaMalloc(&table_, sizeof(double*) * table_cap_));
+    host_.reserve(table_cap_);
+}
+
 PanelStore::~PanelStore() {
     for (double* p : host_) cudaFree(p);
     cudaFree(table_);
@@ -526,56 +568,27 @@ PanelStore::~PanelStore() {
 void PanelStore::ensure_columns(int cols) {
     const int need = (cols + 31) / 32;
     if (need <= panels()) return;
+    if (need > table_cap_) throw std::length_error("basis exceeds the panel table capacity");
+    const int first = panels();
     while (panels() < need) {
         double* p = nullptr;
         AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * 32 * static_cast<size_t>(n_)));
         AMFLS_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * 32 * static_cast<size_t>(n_), stream_));
         host_.push_back(p);
     }
-    if (need > table_cap_) {
-        int cap = std::max(64, table_cap_);
-        while (cap < need) cap *= 2;
-        double** t = nullptr;
-        AMFLS_CUDA(cudaMalloc(&t, sizeof(double*) * cap));
-        if (table_) {
-            AMFLS_CUDA(cudaStreamSynchronize(stream_));
-            cudaFree(table_);
-        }
-        table_ = t;
-        table_cap_ = cap;
-    }
-    AMFLS_CUDA(cudaMemcpyAsync(table_, host_.data(), sizeof(double*) * host_.size(),
-                               cudaMemcpyHostToDevice, stream_));
-    // the host vector may be reallocated by a later push_back before the copy
-    // runs, so make the copy complete now
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    // host_ never reallocates (reserved to table_cap_), so the async copy
+    // reads stable memory
+    AMFLS_CUDA(cudaMemcpyAsync(table_ + first, host_.data() + first,
+                               sizeof(double*) * (need - first), cudaMemcpyHostToDevice, stream_));
 }
-
-// ------------------------------------------------------------ timing ----
-
-struct LevelTiming {
-    std::vector<cudaEvent_t> pool;
-    size_t used = 0;
-    std::vector<std::pair<int, int>> at_pairs, a_pairs;  // event indices
-    cudaEvent_t get() {
-        if (used == pool.size()) {
-            cudaEvent_t e;
-            AMFLS_CUDA(cudaEventCreate(&e));
-            pool.push_back(e);
-        }
-        return pool[used++];
-    }
-    ~LevelTiming() {
-        for (auto e : pool) cudaEventDestroy(e);
-    }
-};
 
 // --------------------------------------------------------- workspace ----
 
 Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regularization,
-                     int maximum_basis_size, cudaStream_t stream, bool time_operators)
+                     int maximum_basis_size, cudaStream_t stream, bool time_operators,
+                     bool use_graphs)
     : op_(op), stream_(stream), m_(op.rows()), n_(op.cols()), reg_(regularization),
-      time_ops_(time_operators), b_(d_b) {
+      time_ops_(time_operators), use_graphs_(use_graphs), b_(d_b) {
     if (m_ <= 0 || n_ <= 0) throw std::invalid_argument("block Golub-Kahan operator dimensions must be positive");
     if (d_b == nullptr) throw std::invalid_argument("block Golub-Kahan right-hand side must not be null");
     if (!std::isfinite(regularization) || regularization < 0.0)
@@ -583,7 +596,6 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     if (maximum_basis_size < 0) throw std::invalid_argument("block Golub-Kahan basis limit must be nonnegative");
     const int mn = std::min(m_, n_);
     basis_limit_ = maximum_basis_size > 0 ? std::min(maximum_basis_size, mn) : mn;
-    timing_ = std::make_unique<LevelTiming>();
     AMFLS_CUDA(cudaMalloc(&dstate_, sizeof(DevState)));
     AMFLS_CUDA(cudaMalloc(&red_, sizeof(RedResult) * 4));
     // scratch: V^T r partials ((target blocks + panels) x 32), then the
@@ -595,27 +607,30 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     const long long ncounters = 64 + max_panels + 64;
     AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * ncounters));
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * ncounters, stream_));
-    AMFLS_CUDA(cudaMalloc(&zeros_n_, sizeof(double) * n_));
-    AMFLS_CUDA(cudaMemsetAsync(zeros_n_, 0, sizeof(double) * n_, stream_));
     AMFLS_CUDA(cudaMalloc(&R_, sizeof(double) * n_));
     AMFLS_CUDA(cudaMalloc(&vnew_, sizeof(double) * n_));
     AMFLS_CUDA(cudaMalloc(&Y_, sizeof(double) * m_));
     ucap_ = 1;
     AMFLS_CUDA(cudaMalloc(&U_, sizeof(double) * m_ * ucap_));
-    V_ = std::make_unique<PanelStore>(n_, stream_);
+    V_ = std::make_unique<PanelStore>(n_, static_cast<int>(max_panels), stream_);
+    V_->ensure_columns(1);  // panel 0 exists (zeroed) before any level runs
+    AMFLS_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
     std::memset(&host_, 0, sizeof(host_));
     host_.reliable = 1;
     host_.basis_limit = basis_limit_;
     AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
 }
 
 Workspace::~Workspace() {
     cudaStreamSynchronize(stream_);
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (capture_stream_) cudaStreamDestroy(capture_stream_);
     cudaFree(dstate_);
     cudaFree(red_);
     cudaFree(partials_);
     cudaFree(counter_);
-    cudaFree(zeros_n_);
     cudaFree(R_);
     cudaFree(vnew_);
     cudaFree(Y_);
@@ -634,6 +649,7 @@ void Workspace::ensure_t_capacity(int cols) {
     if (cols + 2 <= tcap_ && cols <= ccap_) return;
     int cap = std::max(1024, tcap_);
     while (cap < cols + 2) cap *= 2;
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
     auto grow = [&](double*& p, size_t old_count, size_t new_count) {
         double* q = nullptr;
         AMFLS_CUDA(cudaMalloc(&q, sizeof(double) * new_count));
@@ -660,6 +676,20 @@ void Workspace::ensure_t_capacity(int cols) {
     AMFLS_CUDA(cudaMemsetAsync(qr_state_, 0, sizeof(double) * 8, stream_));
     tcap_ = cap;
     ccap_ = cap;
+    invalidate_graph();  // captured kernels hold the old buffer addresses
+}
+
+void Workspace::invalidate_graph() {
+    if (graph_exec_) {
+        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+    }
+    if (graph_) {
+        cudaGraphDestroy(graph_);
+        graph_ = nullptr;
+    }
+    graph_pcap_ = 0;
 }
 
 void Workspace::initialize(const double* d_aux, int aux_cols) {
@@ -692,8 +722,7 @@ void Workspace::initialize(const double* d_aux, int aux_cols) {
     }
     std::memset(&host_.audit, 0, sizeof(host_.audit));
     AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
-    host_expected_k_ = host_.k;
-    host_expected_depth_ = host_.depth;
+    AMFLS_CUDA(cudaStreamSynchronize(stream_));
     if (b_norm_ > 0.0 && aux_cols > 0) append_left_seed(d_aux, aux_cols);
 }
 
@@ -707,58 +736,42 @@ bool Workspace::block_level() {
     throw std::runtime_error("block (width > 1) levels are not available in this build");
 }
 
-void Workspace::enqueue_width_one_level() {
-    const int k = host_expected_k_;
-    ensure_t_capacity(k + 2);
-    V_->ensure_columns(k + 1);
-    // timing events around the two operator calls
-    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
-    level_begin_kernel<<<1, 32, 0, stream_>>>(dstate_, host_expected_depth_ + 1);
+// The kernels of one width-one level.  Every per-level value (k, the
+// previous right column, the depth target) is read from DevState, so the
+// same launches serve every level and can be captured once.
+void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
+    level_begin_kernel<<<1, 32, 0, s>>>(dstate_);
     AMFLS_CUDA(cudaGetLastError());
     // A^T u - beta v_prev
     Epilogue ep;
     ep.out = R_;
-    ep.sub = k > 0 ? V_->column(k - 1) : zeros_n_;
-    ep.sub_stride = k > 0 ? 32 : 1;
+    ep.sub_table = V_->device_table();
+    ep.sub_col = &dstate_->sub_col;
     ep.coef = &dstate_->coupling_eff;
     ep.red = &red_[0];
     ep.guard = &dstate_->go;
     ep.partials = partials_;
     ep.counter = counter_ + 2;
-    if (time_ops_) {
-        e0 = timing_->get();
-        AMFLS_CUDA(cudaEventRecord(e0, stream_));
-    }
-    if (!op_.product1(true, U_, ep, stream_)) {
-        throw std::runtime_error("operator has no fused device product");
-    }
-    if (time_ops_) {
-        e1 = timing_->get();
-        AMFLS_CUDA(cudaEventRecord(e1, stream_));
-        timing_->at_pairs.emplace_back((int)(timing_->used - 2), (int)(timing_->used - 1));
-    }
-    right_scales_kernel<<<1, 32, 0, stream_>>>(dstate_, &red_[0], m_, n_, k == 0 ? 1 : 0);
+    if (!op_.product1(true, U_, ep, s)) throw std::runtime_error("operator has no fused device product");
+    right_scales_kernel<<<1, 32, 0, s>>>(dstate_, &red_[0], m_, n_);
     AMFLS_CUDA(cudaGetLastError());
-    if (k > 0) {
-        const int P = (k + 31) / 32;
-        const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
-        const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + P - 1) / P));
-        const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
-        const dim3 tgrid(P, chunks);
-        const int ngrid = (int)((n_ + 31) / 32);
-        for (int pass = 1; pass <= 2; ++pass) {
-            double* c = pass == 1 ? c1_ : c2_;
-            vt_r_kernel<<<tgrid, kThreads, 0, stream_>>>(V_->device_table(), n_, k, chunk_rows, R_,
-                                                         c, partials_, counter_ + 64, dstate_, pass);
-            AMFLS_CUDA(cudaGetLastError());
-            v_c_kernel<<<ngrid, kThreads, 0, stream_>>>(
-                V_->device_table(), n_, k, c, R_, R_, 1, partials_ + vc_partials_offset_,
-                counter_ + 3, dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, 1, pass);
-            AMFLS_CUDA(cudaGetLastError());
-        }
+    const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
+    const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + pcap - 1) / pcap));
+    const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
+    const dim3 tgrid(pcap, chunks);
+    const int ngrid = (int)((n_ + 31) / 32);
+    for (int pass = 1; pass <= 2; ++pass) {
+        double* c = pass == 1 ? c1_ : c2_;
+        vt_r_kernel<<<tgrid, kThreads, 0, s>>>(V_->device_table(), n_, chunk_rows, R_, c, partials_,
+                                               counter_ + 64, dstate_, pass);
+        AMFLS_CUDA(cudaGetLastError());
+        v_c_kernel<<<ngrid, kThreads, 0, s>>>(
+            V_->device_table(), n_, -1, c, R_, R_, 1, partials_ + vc_partials_offset_, counter_ + 3,
+            dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, 1, pass);
+        AMFLS_CUDA(cudaGetLastError());
     }
-    normalize_right_kernel<<<(int)std::min<long long>(1216, (n_ + 255) / 256), 256, 0, stream_>>>(
-        R_, n_, V_->column(k), vnew_, dstate_);
+    normalize_right_kernel<<<(int)std::min<long long>(1216, (n_ + 255) / 256), 256, 0, s>>>(
+        R_, n_, V_->device_table(), vnew_, dstate_);
     AMFLS_CUDA(cudaGetLastError());
     // y = A v - ||r|| u, with ||A v||, ||y||, u.y
     Epilogue el;
@@ -771,29 +784,49 @@ void Workspace::enqueue_width_one_level() {
     el.guard = &dstate_->go;
     el.partials = partials_;
     el.counter = counter_ + 2;
-    if (time_ops_) {
-        e2 = timing_->get();
-        AMFLS_CUDA(cudaEventRecord(e2, stream_));
-    }
-    op_.product1(false, vnew_, el, stream_);
-    if (time_ops_) {
-        e3 = timing_->get();
-        AMFLS_CUDA(cudaEventRecord(e3, stream_));
-        timing_->a_pairs.emplace_back((int)(timing_->used - 2), (int)(timing_->used - 1));
-    }
-    (void)e0; (void)e1; (void)e2; (void)e3;
+    op_.product1(false, vnew_, el, s);
     const int lgrid = (int)std::max<long long>(1, std::min<long long>(1216, (m_ + 1023) / 1024));
     for (int pass = 1; pass <= 2; ++pass) {
-        left_pass_kernel<<<lgrid, kThreads, 0, stream_>>>(Y_, U_, b_, m_, &red_[1], partials_,
-                                                          counter_ + 4, dstate_, pass, n_, alpha_,
-                                                          beta_, g_);
+        left_pass_kernel<<<lgrid, kThreads, 0, s>>>(Y_, U_, b_, m_, &red_[1], partials_,
+                                                    counter_ + 4, dstate_, pass, n_, alpha_, beta_,
+                                                    g_);
         AMFLS_CUDA(cudaGetLastError());
     }
-    normalize_left_kernel<<<(int)std::min<long long>(1216, (m_ + 255) / 256), 256, 0, stream_>>>(
+    normalize_left_kernel<<<(int)std::min<long long>(1216, (m_ + 255) / 256), 256, 0, s>>>(
         Y_, U_, m_, dstate_);
     AMFLS_CUDA(cudaGetLastError());
-    host_expected_k_ += 1;
-    host_expected_depth_ += 1;
+}
+
+void Workspace::build_graph(int pcap) {
+    invalidate_graph();
+    AMFLS_CUDA(cudaGraphCreate(&graph_, 0));
+    cudaGraphConditionalHandle handle;
+    AMFLS_CUDA(cudaGraphConditionalHandleCreate(&handle, graph_, 1, cudaGraphCondAssignDefault));
+    // the params union has no default constructor: build it in zeroed storage
+    alignas(cudaGraphNodeParams) unsigned char storage[sizeof(cudaGraphNodeParams)] = {};
+    auto* params = reinterpret_cast<cudaGraphNodeParams*>(storage);
+    params->type = cudaGraphNodeTypeConditional;
+    params->conditional.handle = handle;
+    params->conditional.type = cudaGraphCondTypeWhile;
+    params->conditional.size = 1;
+    cudaGraphNode_t node;
+    AMFLS_CUDA(cudaGraphAddNode(&node, graph_, nullptr, nullptr, 0, params));
+    cudaGraph_t body = params->conditional.phGraph_out[0];
+    AMFLS_CUDA(cudaStreamBeginCaptureToGraph(capture_stream_, body, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeRelaxed));
+    try {
+        enqueue_level_kernels(capture_stream_, pcap);
+        level_end_kernel<<<1, 32, 0, capture_stream_>>>(dstate_, handle);
+        AMFLS_CUDA(cudaGetLastError());
+    } catch (...) {
+        cudaGraph_t dummy;
+        cudaStreamEndCapture(capture_stream_, &dummy);
+        throw;
+    }
+    cudaGraph_t captured;
+    AMFLS_CUDA(cudaStreamEndCapture(capture_stream_, &captured));
+    AMFLS_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+    graph_pcap_ = pcap;
 }
 
 void Workspace::advance_to(int target_depth) {
@@ -804,16 +837,24 @@ void Workspace::advance_to(int target_depth) {
         }
         return;
     }
-    host_expected_k_ = host_.k;
-    host_expected_depth_ = host_.depth;
     int levels = target_depth - host_.depth;
     levels = std::min(levels, basis_limit_ - host_.k);
-    if (levels <= 0) return;
-    // all allocations for the run happen before the first launch, so the
-    // enqueue loop never waits for the device
+    if (levels <= 0 || !can_advance()) return;
+    // all allocations for the run happen before the launch, so the device
+    // runs the whole interval without the host
     ensure_t_capacity(host_.k + levels + 2);
     V_->ensure_columns(host_.k + levels + 1);
-    for (int i = 0; i < levels; ++i) enqueue_width_one_level();
+    const int pneed = (host_.k + levels + 31) / 32;
+    int pcap = 4;
+    while (pcap < pneed) pcap *= 2;
+    set_target_kernel<<<1, 32, 0, stream_>>>(dstate_, target_depth, levels);
+    AMFLS_CUDA(cudaGetLastError());
+    if (!use_graphs_) {  // same kernels, launched one by one
+        for (int i = 0; i < levels; ++i) enqueue_level_kernels(stream_, pcap);
+        return;
+    }
+    if (!graph_exec_ || pcap > graph_pcap_) build_graph(pcap);
+    AMFLS_CUDA(cudaGraphLaunch(graph_exec_, stream_));
 }
 
 bool Workspace::advance_level() {
@@ -829,26 +870,10 @@ void Workspace::sync() {
 }
 
 void Workspace::take_operator_seconds(double& a_seconds, double& at_seconds) {
-    a_seconds = 0.0;
-    at_seconds = 0.0;
-    if (!time_ops_) {
-        timing_->used = 0;
-        return;
-    }
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
-    auto sum = [&](std::vector<std::pair<int, int>>& pairs) {
-        double t = 0.0;
-        for (auto& p : pairs) {
-            float ms = 0.0f;
-            AMFLS_CUDA(cudaEventElapsedTime(&ms, timing_->pool[p.first], timing_->pool[p.second]));
-            t += ms * 1e-3;
-        }
-        pairs.clear();
-        return t;
-    };
-    at_seconds = sum(timing_->at_pairs);
-    a_seconds = sum(timing_->a_pairs);
-    timing_->used = 0;
+    a_seconds = static_cast<double>(host_.a_ns - seen_a_ns_) * 1e-9;
+    at_seconds = static_cast<double>(host_.at_ns - seen_at_ns_) * 1e-9;
+    seen_a_ns_ = host_.a_ns;
+    seen_at_ns_ = host_.at_ns;
 }
 
 void Workspace::solve_projected(double* d_x) {

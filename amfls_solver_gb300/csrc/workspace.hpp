@@ -11,8 +11,10 @@
 //      as in the reference); P pending P*Omega, m x p.
 //   T  projected operator: lower bidiagonal at width one, kept as the two
 //      diagonals alpha_j = T(j, j), beta_{j+1} = T(j+1, j); g = U^T b.
-// Width-one levels run entirely on the device (DevState decisions); wider
-// blocks use the host-synchronised block path.
+// Width-one levels run entirely on the device (DevState decisions): one level
+// is captured as the body of a CUDA graph WHILE node, so a whole checkpoint
+// interval is a single graph launch.  Wider blocks use the host-synchronised
+// block path.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,7 +30,7 @@ namespace amfls_gpu {
 
 class PanelStore {
 public:
-    PanelStore(int n, cudaStream_t stream) : n_(n), stream_(stream) {}
+    PanelStore(int n, int max_panels, cudaStream_t stream);
     ~PanelStore();
     void ensure_columns(int cols);  // allocate (zeroed) panels to hold `cols` columns
     double* column(int j) const { return host_[j / 32] + (j % 32); }  // stride 32
@@ -45,12 +47,11 @@ private:
     int table_cap_ = 0;
 };
 
-struct LevelTiming;  // events around operator calls
-
 class Workspace {
 public:
     Workspace(const DeviceOperator& op, const double* d_b, double regularization,
-              int maximum_basis_size, cudaStream_t stream, bool time_operators);
+              int maximum_basis_size, cudaStream_t stream, bool time_operators,
+              bool use_graphs = true);
     ~Workspace();
     Workspace(const Workspace&) = delete;
     Workspace& operator=(const Workspace&) = delete;
@@ -96,7 +97,9 @@ public:
     unsigned* scratch_counter() const { return counter_; }
 
 private:
-    void enqueue_width_one_level();
+    void enqueue_level_kernels(cudaStream_t s, int pcap);
+    void build_graph(int pcap);
+    void invalidate_graph();
     bool block_level();
     void ensure_t_capacity(int cols);
 
@@ -107,6 +110,7 @@ private:
     int basis_limit_;
     bool initialized_ = false;
     bool time_ops_;
+    bool use_graphs_;
     const double* b_;   // caller's device b (kept alive by the caller)
     double b_norm_ = 0.0;
 
@@ -116,7 +120,6 @@ private:
     double* partials_ = nullptr;
     long long vc_partials_offset_ = 0;
     unsigned* counter_ = nullptr;   // self-resetting tickets: misc + one per V panel
-    double* zeros_n_ = nullptr;
 
     std::unique_ptr<PanelStore> V_;
     double* U_ = nullptr;      // m x ucap
@@ -138,9 +141,12 @@ private:
     double* qr_ = nullptr;     // rho, theta, phi (3 x tcap) + y (tcap)
     double* qr_state_ = nullptr;  // [c, s, rhobar, phibar, processed]
     int projected_flags_ = 0;
-    int host_expected_k_ = 0;  // k the host expects at the next enqueued level
-    int host_expected_depth_ = 0;
-    std::unique_ptr<LevelTiming> timing_;
+    // one width-one level captured as the body of a device-side WHILE loop
+    cudaStream_t capture_stream_ = nullptr;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    int graph_pcap_ = 0;  // V panels the captured sweep grids cover
+    unsigned long long seen_a_ns_ = 0, seen_at_ns_ = 0;
 };
 
 }  // namespace amfls_gpu

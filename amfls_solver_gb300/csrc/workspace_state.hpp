@@ -55,6 +55,14 @@ struct DevState {
     int left_rank;    // retained next left width of the current level
     int level_ok;     // advance_level's return value for the last run level
     int coeff_nonfinite;
+    int target_depth;     // depth at which the enqueued run of levels stops
+    int iterations_left;  // hard cap on loop iterations of the enqueued run
+    int sub_col;          // V column subtracted by the coupling (0 when none)
+    int pad_state;
+    // device time of search operator calls (globaltimer, ns)
+    unsigned long long a_ns;
+    unsigned long long at_ns;
+    unsigned long long t_mark;
     // operator call counters of executed search levels
     long long search_a_columns;
     long long search_at_columns;

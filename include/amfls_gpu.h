@@ -74,7 +74,10 @@ typedef struct {
     int maximum_auxiliary_width; /* 0 = default */
     int auxiliary_width;         /* fixed RBGK only */
     int stop_early;              /* fixed RBGK only */
-    int time_operators;          /* record CUDA-event times of operator calls (default 1) */
+    int time_operators;          /* record device times of operator calls (default 1) */
+    int use_graphs;              /* run width-one levels as one CUDA graph per checkpoint
+                                    interval (default 1); 0 launches the same kernels one by
+                                    one, e.g. for per-kernel profiling */
 } amfls_gpu_options;
 
 /* LeastSquaresResult, packed like the torch binding's tensors. */
