@@ -32,7 +32,8 @@ class Result(ctypes.Structure):
                 ("basis_rank", ctypes.c_int), ("status", ctypes.c_int),
                 ("stop_reason", ctypes.c_int), ("metrics", ctypes.c_double * METRICS),
                 ("counters", ctypes.c_longlong * COUNTERS),
-                ("timings", ctypes.c_double * TIMINGS), ("trace_rows", ctypes.c_int)]
+                ("timings", ctypes.c_double * TIMINGS), ("trace_rows", ctypes.c_int),
+                ("kernel_launches", ctypes.c_longlong)]
 
 
 class ValidationModel(ctypes.Structure):

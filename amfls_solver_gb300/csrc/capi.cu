@@ -86,6 +86,7 @@ void export_result(const amfls_gpu::SolveResult& r, amfls_gpu_result* out, doubl
     amfls_gpu::pack_counters(r, out->counters);
     amfls_gpu::pack_timings(r, out->timings);
     out->trace_rows = static_cast<int>(r.trace.size());
+    out->kernel_launches = r.statistics.kernel_launches;
     const int rows = std::min<int>(cap, static_cast<int>(r.trace.size()));
     for (int i = 0; i < rows; ++i) {
         if (tf) std::memcpy(tf + 29 * i, r.trace[i].f, sizeof(double) * 29);

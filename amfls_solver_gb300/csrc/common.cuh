@@ -23,6 +23,19 @@ inline void check_cuda(cudaError_t e, const char* what) {
 
 #define AMFLS_CUDA(call) ::amfls_gpu::check_cuda((call), #call)
 
+// Kernel launches made by this thread (reported per solve).  Launch sites
+// use AMFLS_LAUNCHED() right after the <<<...>>> statement.
+inline long long& launch_count() {
+    static thread_local long long count = 0;
+    return count;
+}
+
+#define AMFLS_LAUNCHED()                                             \
+    do {                                                             \
+        ::amfls_gpu::check_cuda(cudaGetLastError(), "kernel launch"); \
+        ++::amfls_gpu::launch_count();                               \
+    } while (0)
+
 constexpr int kWarp = 32;
 constexpr int kPanel = 32;  // columns per V panel (row-major n x 32 tiles)
 

@@ -543,6 +543,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
         throw std::invalid_argument("work limits must be nonnegative");
     const double reg = o.regularization, tol = o.tolerance;
     const auto t_start = Clock::now();
+    const long long launches0 = launch_count();
     Statistics stats;
     Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators, o.use_graphs);
     Evaluator ev(ws, op, d_b, reg, stats, stream);
@@ -604,6 +605,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
                                    cudaMemcpyDeviceToDevice, stream));
         AMFLS_CUDA(cudaStreamSynchronize(stream));
         stats.total_seconds = seconds_since(t_start);
+        stats.kernel_launches = launch_count() - launches0;
         out.statistics = stats;
         return out;
     };
@@ -821,6 +823,7 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
         throw std::length_error("fixed RBGK seed width exceeds LP64 limits");
     const double reg = o.regularization, tol = o.tolerance;
     const auto t_start = Clock::now();
+    const long long launches0 = launch_count();
     Statistics stats;
     Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators, o.use_graphs);
     Evaluator ev(ws, op, d_b, reg, stats, stream);
@@ -960,6 +963,7 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
                                cudaMemcpyDeviceToDevice, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
     stats.total_seconds = seconds_since(t_start);
+    stats.kernel_launches = launch_count() - launches0;
     out.statistics = stats;
     return out;
 }

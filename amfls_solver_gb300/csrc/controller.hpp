@@ -49,6 +49,7 @@ struct Statistics {
     long long gaussian_random_block_requests = 0;
     // GB300 extras (not in the reference's tensors)
     long long projected_rank_flags = 0;
+    long long kernel_launches = 0;  // kernels this solve ran on the GPU
 };
 
 struct TraceRow {

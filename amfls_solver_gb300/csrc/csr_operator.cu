@@ -429,7 +429,7 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
 
     check_offsets_kernel<<<setup_grid(rows_), 256, 0, stream>>>(
         A.off, rows_, nnz, &w->err, &w->max_len_r, lens, elems_per_lane_, bins);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     int err = 0;
     AMFLS_CUDA(cudaMemcpyAsync(&err, &w->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
@@ -449,7 +449,7 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
 
     expand_rows_kernel<<<setup_grid(rows_), 256, 0, stream>>>(A.off, d_idx, d_val, rows_, cols_,
                                                               A.idx, row_of, &w->err);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     AMFLS_CUDA(cudaMemcpyAsync(&err, &w->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
     if (err & 4) fail("CSR column index is out of range");
@@ -459,7 +459,7 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
     AMFLS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (cols_ + 1), stream));
     if (nnz > 0) {
         count_columns_kernel<<<setup_grid(nnz), 256, 0, stream>>>(A.idx, nnz, counts);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
         int* keys_sorted = nullptr;
         AMFLS_CUDA(cudaMallocAsync(&keys_sorted, sizeof(int) * nnz, stream));
         int* ids = perm;  // entry ids 0..nnz-1, the sort's payload
@@ -477,7 +477,7 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
                                                    perm_out, (int)nnz, 0, bits, stream));
         gather_transpose_kernel<<<setup_grid(nnz), 256, 0, stream>>>(perm_out, row_of, A.val, nnz,
                                                                      T.idx, T.val);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
         AMFLS_CUDA(cudaFreeAsync(tmp, stream));
         AMFLS_CUDA(cudaFreeAsync(perm_out, stream));
         AMFLS_CUDA(cudaFreeAsync(keys_sorted, stream));
@@ -493,7 +493,7 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
         AMFLS_CUDA(cudaFreeAsync(tmp, stream));
     }
     duplicate_kernel<<<setup_grid(cols_), 256, 0, stream>>>(T.off, T.idx, cols_, &w->err);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     AMFLS_CUDA(cudaMemcpyAsync(&err, &w->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
     if (err & 16) fail("CSR rows must not contain duplicate columns");
@@ -501,21 +501,21 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
     // transpose bins
     check_offsets_kernel<<<setup_grid(cols_), 256, 0, stream>>>(
         T.off, cols_, nnz, &w->err, &w->max_len_c, lens, elems_per_lane_, bins);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     build_bins(T, bins, stream);
 
     // certified norm model
     norm_model_kernel<<<setup_grid(rows_), 256, 0, stream>>>(A.off, A.val, rows_, 0, w->row_acc,
                                                             nullptr, nullptr, nullptr);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     const int cgrid = setup_grid(cols_);
     double* frob_partials = nullptr;
     AMFLS_CUDA(cudaMallocAsync(&frob_partials, sizeof(double) * cgrid, stream));
     norm_model_kernel<<<cgrid, 256, 0, stream>>>(T.off, T.val, cols_, 1, w->col_acc,
                                                  frob_partials, counter_, &w->frob2);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     finish_model_kernel<<<1, 1, 0, stream>>>(w->row_acc, w->col_acc, &w->frob2, w->model);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     Work host{};
     AMFLS_CUDA(cudaMemcpyAsync(&host, w, sizeof(Work), cudaMemcpyDeviceToHost, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
@@ -546,7 +546,7 @@ __global__ void fill_ids_kernel(int* ids, long long n) {
 
 void CsrOperator::fill_ids(int* ids, long long n, cudaStream_t stream) {
     fill_ids_kernel<<<setup_grid(n), 256, 0, stream>>>(ids, n);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 bool CsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
@@ -556,7 +556,7 @@ bool CsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
     spmv_binned_kernel<<<grid, kThreads, 0, stream>>>(
         s.off, s.idx, s.val, s.perm, s.bins, x, ep,
         ep.partials ? ep.partials : scratch_, ep.counter ? ep.counter : counter_);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     return true;
 }
 
@@ -578,7 +578,7 @@ void CsrOperator::product(bool transpose, const double* x, int block_cols, doubl
         const int nc = std::min(8, block_cols - c0);
         spmm_binned_kernel<8><<<grid, kThreads, 0, stream>>>(
             s.off, s.idx, s.val, s.perm, s.bins, x + c0 * ldx, ldx, y + c0 * ldy, ldy, nc);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
     }
 }
 
@@ -596,7 +596,7 @@ void CsrOperator::refined(bool transpose, const double* x_hi, const double* x_lo
     const Side& s = transpose ? *t_ : *a_;
     spmv_dd_kernel<<<grid_for(s.bins.warp_start[6]), kThreads, 0, stream>>>(
         s.off, s.idx, s.val, s.perm, s.bins, x_hi, x_lo, y_hi, y_lo, finite);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 void CsrOperator::apply_refined(const double* x_hi, const double* x_lo, double* y_hi,

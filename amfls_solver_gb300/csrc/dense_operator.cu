@@ -235,7 +235,7 @@ void split_chunks(int out_n, int in_n, int& chunks, int& chunk) {
 void run_epilogue(const double* t, long long n, const Epilogue& ep, double* partials,
                   unsigned* counter, cudaStream_t s) {
     epilogue_kernel<<<grid_1d(n), kThreads, 0, s>>>(t, n, ep, partials, counter);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool column_major,
@@ -266,12 +266,14 @@ DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool co
     AMFLS_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * (9 + ig + og), stream));
     model_outer_kernel<<<og, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9 + ig, counter_ + 2,
                                                     w + 8);
+    AMFLS_LAUNCHED();
     model_inner_kernel<<<ig, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9, counter_, w + 5);
+    AMFLS_LAUNCHED();
     // the reference's Frobenius bound sums column square sums: the inner
     // index for row-major storage, the outer one for column-major
     model_finish_kernel<<<1, 1, 0, stream>>>(w, column_major ? w + 8 : w + 5,
                                              column_major ? 0 : 1, w + 6);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     double model[2];
     AMFLS_CUDA(cudaMemcpyAsync(model, w + 6, sizeof(model), cudaMemcpyDeviceToHost, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
@@ -302,6 +304,7 @@ void DenseOperator::product(bool transpose, const double* x, double* y, const in
         const long long warps = out_n;
         const int grid = (int)std::max<long long>(1, std::min<long long>(kTargetBlocks * 2, (warps + 7) / 8));
         dot_rows_kernel<<<grid, kThreads, 0, s>>>(a_, ld, out_n, in_n, x, y, guard);
+        AMFLS_LAUNCHED();
     } else {
         int chunks = 0, chunk = 0;
         split_chunks(out_n, in_n, chunks, chunk);
@@ -310,9 +313,11 @@ void DenseOperator::product(bool transpose, const double* x, double* y, const in
             throw std::logic_error("dense operator partial buffer is too small");
         sum_cols_kernel<<<dim3(oblocks, chunks), kThreads, 0, s>>>(a_, ld, out_n, in_n, chunk, x,
                                                                    partials_, guard);
+        AMFLS_LAUNCHED();
         add_chunks_kernel<<<grid_1d(out_n), kThreads, 0, s>>>(partials_, chunks, out_n, y, guard);
+        AMFLS_LAUNCHED();
     }
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 void DenseOperator::apply(const double* x, int block_cols, double* y, cudaStream_t s) const {
@@ -341,11 +346,13 @@ void DenseOperator::apply_refined(const double* x_hi, const double* x_lo, double
     if (!column_major_) {
         dd_dot_rows_kernel<<<grid_1d((long long)rows_ * 32), kThreads, 0, s>>>(
             a_, cols_, rows_, cols_, x_hi, x_lo, y_hi, y_lo, finite);
+        AMFLS_LAUNCHED();
     } else {
         dd_sum_cols_kernel<<<grid_1d(rows_), kThreads, 0, s>>>(a_, rows_, rows_, cols_, x_hi,
                                                                x_lo, y_hi, y_lo, finite);
+        AMFLS_LAUNCHED();
     }
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 void DenseOperator::apply_transpose_refined(const double* y_hi, const double* y_lo, double* x_hi,
@@ -353,11 +360,13 @@ void DenseOperator::apply_transpose_refined(const double* y_hi, const double* y_
     if (column_major_) {
         dd_dot_rows_kernel<<<grid_1d((long long)cols_ * 32), kThreads, 0, s>>>(
             a_, rows_, cols_, rows_, y_hi, y_lo, x_hi, x_lo, finite);
+        AMFLS_LAUNCHED();
     } else {
         dd_sum_cols_kernel<<<grid_1d(cols_), kThreads, 0, s>>>(a_, cols_, cols_, rows_, y_hi,
                                                                y_lo, x_hi, x_lo, finite);
+        AMFLS_LAUNCHED();
     }
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 }  // namespace amfls_gpu

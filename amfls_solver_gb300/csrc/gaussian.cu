@@ -62,7 +62,7 @@ void gaussian_block(int rows, int cols, std::uint64_t seed, std::uint64_t stream
     const int grid = (int)std::min<long long>(2432, (total + 255) / 256);
     gaussian_kernel<<<grid, 256, 0, s>>>(rows, cols, gaussian_key(seed, stream), first_column,
                                          d_out, ld);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 }  // namespace amfls_gpu
@@ -104,11 +104,11 @@ void project_out_direction(double* R, int rows, int cols, const double* b, doubl
     double* dots = nullptr;
     AMFLS_CUDA(cudaMallocAsync(&dots, sizeof(double) * cols, s));
     direction_dots_kernel<<<std::min(cols, 1216), 256, 0, s>>>(R, rows, cols, b, bnorm, dots);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     const long long total = (long long)rows * cols;
     direction_update_kernel<<<(int)std::min<long long>(2432, (total + 255) / 256), 256, 0, s>>>(
         R, rows, cols, b, bnorm, dots);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     AMFLS_CUDA(cudaFreeAsync(dots, s));
 }
 

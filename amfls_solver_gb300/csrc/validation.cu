@@ -657,9 +657,13 @@ struct Validator::Impl {
         if (op.product1(transpose, x, ep, stream)) return;
         if (transpose) op.apply_transpose(x, 1, t_out, stream);
         else op.apply(x, 1, t_out, stream);
-        if (minus) sub_kernel<<<vgrid(m), 256, 0, stream>>>(t_out, minus, out, m);
-        if (fma_vec) fma_kernel<<<vgrid(n), 256, 0, stream>>>(reg, fma_vec, t_out, out, n);
-        AMFLS_CUDA(cudaGetLastError());
+        if (minus) { sub_kernel<<<vgrid(m), 256, 0, stream>>>(t_out, minus, out, m);
+            AMFLS_LAUNCHED();
+        }
+        if (fma_vec) {
+            fma_kernel<<<vgrid(n), 256, 0, stream>>>(reg, fma_vec, t_out, out, n);
+            AMFLS_LAUNCHED();
+        }
     }
 
     void norms(NormResult* dst, std::initializer_list<std::pair<const double*, long long>> vecs) {
@@ -694,7 +698,7 @@ struct Validator::Impl {
         norms(&vs->nr, {{b, m}, {x, n}, {ax, m}, {r, m}, {atr, n}, {g, n}});
         base_contract_kernel<<<1, 32, 0, stream>>>(vs, mdl, m, n, reg, tol,
                                                    op.supports_validation_refinement() ? 1 : 0);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
         ValState h = read();
         const double* grad = g;
         if (h.need_refine) {
@@ -717,22 +721,23 @@ struct Validator::Impl {
             calls[2] = 1;
             dd_residual_kernel<<<vgrid(m), 256, 0, stream>>>(hi1, lo1, b, rn_hi, rn_lo, m,
                                                              &vs->finite_flag);
+            AMFLS_LAUNCHED();
             timed_begin();
             op.apply_transpose_refined(rn_hi, rn_lo, hi2, lo2, &vs->finite_flag, stream);
             sec[3] = timed_end();
             calls[3] = 1;
             dd_gradient_kernel<<<vgrid(n), 256, 0, stream>>>(reg, x, hi2, lo2, g2, n,
                                                              &vs->finite_flag);
-            AMFLS_CUDA(cudaGetLastError());
+            AMFLS_LAUNCHED();
             norms(&vs->nr2, {{b, m}, {x, n}, {hi1, m}, {rn_hi, m}, {hi2, n}, {g2, n}});
             refined_contract_kernel<<<1, 32, 0, stream>>>(vs, mdl, m, n, reg, tol);
-            AMFLS_CUDA(cudaGetLastError());
+            AMFLS_LAUNCHED();
             h = read();
             if (h.need_refine) grad = g2;  // refined vectors replace the base ones
         }
         if (reg > 0.0) {
             ridge_prelim_kernel<<<1, 32, 0, stream>>>(vs, reg);
-            AMFLS_CUDA(cudaGetLastError());
+            AMFLS_LAUNCHED();
             h = read();
             if (h.need_correction) {
                 // d = g / ||g||, A d, A^T A d + lambda d, d.h, q = g - step h
@@ -743,12 +748,14 @@ struct Validator::Impl {
                 AMFLS_CUDA(cudaMallocAsync(&hv, sizeof(double) * n, stream));
                 AMFLS_CUDA(cudaMallocAsync(&q, sizeof(double) * n, stream));
                 scale_kernel<<<vgrid(n), 256, 0, stream>>>(grad, vs, d, n);
+                AMFLS_LAUNCHED();
                 timed_begin();
                 product(false, d, ad, ad, nullptr, nullptr);
                 sec[4] = timed_end();
                 calls[4] = 1;
                 norms(&vs->nr2, {{d, n}, {ad, m}});
                 correction_step_kernel<<<1, 32, 0, stream>>>(vs, mdl, m, n, reg, 0);
+                AMFLS_LAUNCHED();
                 h = read();
                 if (h.need_correction) {
                     timed_begin();
@@ -757,6 +764,7 @@ struct Validator::Impl {
                     calls[5] = 1;
                     dot_kernel<<<vgrid(n), 256, 0, stream>>>(d, hv, n, partials, counters + 9,
                                                              &vs->dot);
+                    AMFLS_LAUNCHED();
                     VectorSet set{};
                     set.v[0] = d; set.n[0] = n;
                     set.v[1] = ad; set.n[1] = m;
@@ -764,9 +772,11 @@ struct Validator::Impl {
                     set.count = 3;
                     norm_passes(set, &vs->nr2, partials, counters, stream);
                     correction_step_kernel<<<1, 32, 0, stream>>>(vs, mdl, m, n, reg, 1);
+                    AMFLS_LAUNCHED();
                     h = read();
                     if (h.need_correction) {
                         correction_q_kernel<<<vgrid(n), 256, 0, stream>>>(hv, grad, vs, q, n);
+                        AMFLS_LAUNCHED();
                         VectorSet s2{};
                         s2.v[0] = d; s2.n[0] = n;
                         s2.v[1] = ad; s2.n[1] = m;
@@ -775,7 +785,7 @@ struct Validator::Impl {
                         s2.count = 4;
                         norm_passes(s2, &vs->nr2, partials, counters, stream);
                         correction_step_kernel<<<1, 32, 0, stream>>>(vs, mdl, m, n, reg, 2);
-                        AMFLS_CUDA(cudaGetLastError());
+                        AMFLS_LAUNCHED();
                     }
                 }
                 AMFLS_CUDA(cudaFreeAsync(hv, stream));
@@ -783,7 +793,7 @@ struct Validator::Impl {
             }
         }
         finish_kernel<<<1, 32, 0, stream>>>(vs, reg, tol);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
         h = read();
         ValidationOutput out = h.out;
         for (int i = 0; i < 6; ++i) {

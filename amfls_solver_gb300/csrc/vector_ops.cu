@@ -87,9 +87,9 @@ void norm_passes(const VectorSet& set, NormResult* out, double* partials, unsign
     for (int i = 0; i < set.count; ++i) longest = std::max(longest, set.n[i]);
     const int grid = (int)std::max<long long>(1, std::min<long long>(kGrid, (longest + 1023) / 1024));
     max_pass_kernel<<<grid, kThreads, 0, stream>>>(set, out, partials, counter);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     sum_pass_kernel<<<grid, kThreads, 0, stream>>>(set, out, partials, counter);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 double euclid_from(const NormResult& r, int i) {

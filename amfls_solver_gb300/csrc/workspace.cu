@@ -176,6 +176,7 @@ __global__ void set_target_kernel(DevState* st, int target_depth, int iterations
 
 __global__ void level_begin_kernel(DevState* st) {
     if (threadIdx.x != 0) return;
+    st->body_runs += 1;
     const bool go = can_advance_dev(st) && st->iterations_left > 0;
     st->iterations_left -= 1;
     st->go = go ? 1 : 0;
@@ -714,7 +715,7 @@ void Workspace::initialize(const double* d_aux, int aux_cols) {
         const double inv = 1.0 / b_norm_;
         scale_copy_kernel<<<std::max<long long>(1, std::min<long long>(1216, (m_ + 255) / 256)), 256, 0,
                             stream_>>>(b_, U_, m_, inv);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
         AMFLS_CUDA(cudaMemcpyAsync(g_, &b_norm_, sizeof(double), cudaMemcpyHostToDevice, stream_));
         host_.left_width = 1;
         host_.rows_t = 1;
@@ -741,7 +742,7 @@ bool Workspace::block_level() {
 // same launches serve every level and can be captured once.
 void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     level_begin_kernel<<<1, 32, 0, s>>>(dstate_);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     // A^T u - beta v_prev
     Epilogue ep;
     ep.out = R_;
@@ -754,7 +755,7 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     ep.counter = counter_ + 2;
     if (!op_.product1(true, U_, ep, s)) throw std::runtime_error("operator has no fused device product");
     right_scales_kernel<<<1, 32, 0, s>>>(dstate_, &red_[0], m_, n_);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
     const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + pcap - 1) / pcap));
     const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
@@ -764,15 +765,15 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
         double* c = pass == 1 ? c1_ : c2_;
         vt_r_kernel<<<tgrid, kThreads, 0, s>>>(V_->device_table(), n_, chunk_rows, R_, c, partials_,
                                                counter_ + 64, dstate_, pass);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
         v_c_kernel<<<ngrid, kThreads, 0, s>>>(
             V_->device_table(), n_, -1, c, R_, R_, 1, partials_ + vc_partials_offset_, counter_ + 3,
             dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, 1, pass);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
     }
     normalize_right_kernel<<<(int)std::min<long long>(1216, (n_ + 255) / 256), 256, 0, s>>>(
         R_, n_, V_->device_table(), vnew_, dstate_);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     // y = A v - ||r|| u, with ||A v||, ||y||, u.y
     Epilogue el;
     el.out = Y_;
@@ -790,11 +791,11 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
         left_pass_kernel<<<lgrid, kThreads, 0, s>>>(Y_, U_, b_, m_, &red_[1], partials_,
                                                     counter_ + 4, dstate_, pass, n_, alpha_, beta_,
                                                     g_);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
     }
     normalize_left_kernel<<<(int)std::min<long long>(1216, (m_ + 255) / 256), 256, 0, s>>>(
         Y_, U_, m_, dstate_);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
 }
 
 void Workspace::build_graph(int pcap) {
@@ -814,15 +815,19 @@ void Workspace::build_graph(int pcap) {
     cudaGraph_t body = params->conditional.phGraph_out[0];
     AMFLS_CUDA(cudaStreamBeginCaptureToGraph(capture_stream_, body, nullptr, nullptr, 0,
                                              cudaStreamCaptureModeRelaxed));
+    const long long launches_before = launch_count();
     try {
         enqueue_level_kernels(capture_stream_, pcap);
         level_end_kernel<<<1, 32, 0, capture_stream_>>>(dstate_, handle);
-        AMFLS_CUDA(cudaGetLastError());
+        AMFLS_LAUNCHED();
     } catch (...) {
         cudaGraph_t dummy;
         cudaStreamEndCapture(capture_stream_, &dummy);
         throw;
     }
+    // captured launches run once per loop iteration, counted from body_runs
+    body_kernels_ = launch_count() - launches_before;
+    launch_count() = launches_before;
     cudaGraph_t captured;
     AMFLS_CUDA(cudaStreamEndCapture(capture_stream_, &captured));
     AMFLS_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
@@ -848,13 +853,14 @@ void Workspace::advance_to(int target_depth) {
     int pcap = 4;
     while (pcap < pneed) pcap *= 2;
     set_target_kernel<<<1, 32, 0, stream_>>>(dstate_, target_depth, levels);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     if (!use_graphs_) {  // same kernels, launched one by one
         for (int i = 0; i < levels; ++i) enqueue_level_kernels(stream_, pcap);
         return;
     }
     if (!graph_exec_ || pcap > graph_pcap_) build_graph(pcap);
     AMFLS_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+    ++graph_launches_;
 }
 
 bool Workspace::advance_level() {
@@ -867,6 +873,10 @@ bool Workspace::advance_level() {
 void Workspace::sync() {
     AMFLS_CUDA(cudaMemcpyAsync(&host_, dstate_, sizeof(DevState), cudaMemcpyDeviceToHost, stream_));
     AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    if (use_graphs_) {  // kernels the device ran inside graph-launched intervals
+        launch_count() += body_kernels_ * (host_.body_runs - counted_body_runs_);
+    }
+    counted_body_runs_ = host_.body_runs;
 }
 
 void Workspace::take_operator_seconds(double& a_seconds, double& at_seconds) {
@@ -886,12 +896,12 @@ void Workspace::solve_projected(double* d_x) {
     const double rcond = std::min(0.5, 64.0 * kEps * std::max(host_.rows_t, k));
     projected_solve_kernel<<<1, 32, 0, stream_>>>(alpha_, beta_, g_, k, host_.rows_t, reg_, qr_,
                                                   tcap_, qr_state_, rcond);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     const double* y = qr_ + 3 * (long long)tcap_;
     v_c_kernel<<<(int)((n_ + 31) / 32), kThreads, 0, stream_>>>(
         V_->device_table(), n_, k, y, nullptr, d_x, 0, partials_, counter_ + 5, dstate_, kHookNone,
         m_, 0, 1);
-    AMFLS_CUDA(cudaGetLastError());
+    AMFLS_LAUNCHED();
     double st[8];
     AMFLS_CUDA(cudaMemcpyAsync(st, qr_state_, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream_));
     AMFLS_CUDA(cudaStreamSynchronize(stream_));

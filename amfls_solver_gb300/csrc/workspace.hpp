@@ -146,6 +146,9 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_pcap_ = 0;  // V panels the captured sweep grids cover
+    long long body_kernels_ = 0;       // kernels in the captured level body
+    long long counted_body_runs_ = 0;  // body runs already added to launch_count()
+    long long graph_launches_ = 0;
     unsigned long long seen_a_ns_ = 0, seen_at_ns_ = 0;
 };
 

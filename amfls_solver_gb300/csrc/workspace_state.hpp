@@ -63,6 +63,7 @@ struct DevState {
     unsigned long long a_ns;
     unsigned long long at_ns;
     unsigned long long t_mark;
+    long long body_runs;   // executions of the captured level body
     // operator call counters of executed search levels
     long long search_a_columns;
     long long search_at_columns;

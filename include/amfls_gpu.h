@@ -88,6 +88,7 @@ typedef struct {
     long long counters[AMFLS_GPU_COUNTERS];
     double timings[AMFLS_GPU_TIMINGS];
     int trace_rows; /* checkpoints evaluated; rows beyond the capacity are dropped */
+    long long kernel_launches; /* GPU kernels the solve ran (not part of the reference) */
 } amfls_gpu_result;
 
 /* Sets the reference's defaults (amfls.hpp:10-20; fixed_rbgk.hpp:8-18). */
