@@ -50,7 +50,7 @@ EXPORTED = [
     "amfls_gpu_operator_cols", "amfls_gpu_operator_apply", "amfls_gpu_operator_apply_transpose",
     "amfls_gpu_operator_relative_block_product_cost",
     "amfls_gpu_operator_validation_error_model", "amfls_gpu_solve_amfls",
-    "amfls_gpu_solve_fixed_rbgk",
+    "amfls_gpu_solve_fixed_rbgk", "amfls_gpu_dense_apply_transpose_noalloc",
 ]
 
 
@@ -88,6 +88,7 @@ def load():
     lib.amfls_gpu_operator_relative_block_product_cost.argtypes = [P, I]
     lib.amfls_gpu_operator_relative_block_product_cost.restype = D
     lib.amfls_gpu_operator_validation_error_model.argtypes = [P, ctypes.POINTER(ValidationModel)]
+    lib.amfls_gpu_dense_apply_transpose_noalloc.argtypes = [I, I, P, P, P, P]
     for name in ("amfls_gpu_solve_amfls", "amfls_gpu_solve_fixed_rbgk"):
         getattr(lib, name).argtypes = [P, P, ctypes.POINTER(Options), P, ctypes.POINTER(Result),
                                        P, P, I, P]

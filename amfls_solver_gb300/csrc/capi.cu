@@ -102,6 +102,10 @@ const amfls_gpu::DeviceOperator& deref(const amfls_gpu_operator* op) {
 
 }  // namespace
 
+namespace amfls_gpu {
+void set_last_error(const std::string& message) { g_last_error = message; }
+}  // namespace amfls_gpu
+
 extern "C" {
 
 void amfls_gpu_default_options(amfls_gpu_options* o) {

@@ -145,6 +145,21 @@ int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
                                amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
                                int trace_capacity, void* stream);
 
+/* x = A^T y for a row-major dense A (rows x cols) without any device
+ * allocation.  No counterpart in the reference: this is for callers that
+ * cannot call cudaMalloc (code running during CUDA stream capture, real-time
+ * loops that must not synchronise the device, hosts whose memory manager
+ * owns all device memory).  The partial sums live in one fixed 8 MiB array
+ * of device global memory (1,048,576 doubles) that every GPU loading the
+ * library holds until exit; cols above that capacity are rejected with
+ * AMFLS_GPU_LENGTH_ERROR.  The first call on each device looks the array's
+ * device address up (cudaGetSymbolAddress) with that device current, so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls whose kernels may overlap on the GPU (unordered streams) race; calls
+ * ordered on one stream are safe.  Asynchronous on `stream`. */
+int amfls_gpu_dense_apply_transpose_noalloc(int rows, int cols, const double* d_values,
+                                            const double* d_y, double* d_x, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,64 @@
+"""The allocation-free dense transpose product against the regular one.
+
+amfls_gpu_dense_apply_transpose_noalloc serves callers that cannot allocate
+device memory (inside CUDA stream capture, in loops that must not synchronise
+the device, under a host memory manager that owns all device memory).  It
+keeps its partial sums in a fixed device array shared by all calls, so this
+test runs it twice in a row (the second call sees the first call's leftover
+partials) and compares both results with the regular entry point,
+amfls_gpu_operator_apply_transpose on a dense operator, to the product's
+rounding model.  This file sorts last so a stop-at-first-failure run has
+already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def native():
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import _native
+
+    amfls.load_library()
+    return amfls, _native.load()
+
+
+def noalloc_transpose(lib, a, y):
+    x = torch.empty(a.shape[1], dtype=torch.float64, device=a.device)
+    rc = lib.amfls_gpu_dense_apply_transpose_noalloc(
+        a.shape[0], a.shape[1], a.data_ptr(), y.data_ptr(), x.data_ptr(),
+        torch.cuda.current_stream(a.device).cuda_stream)
+    assert rc == 0, lib.amfls_gpu_last_error()
+    return x
+
+
+def test_noalloc_matches_regular_entry_point_twice(native):
+    amfls, lib = native
+    rng = np.random.default_rng(7)
+    a = torch.from_numpy(rng.standard_normal((3000, 700))).cuda()
+    op = amfls.DeviceOperator(a)
+    abs_a = a.abs()
+    for seed in (1, 2):  # two calls in a row share the scratch array
+        y = torch.from_numpy(np.random.default_rng(seed).standard_normal(3000)).cuda()
+        ref = op.apply(y, transpose=True)
+        got = noalloc_transpose(lib, a, y)
+        torch.cuda.synchronize()
+        # gamma_{2 rows + 2} |A|^T |y|: the reference's rounding model for A^T y
+        k = 2 * 3000 + 2
+        u = np.finfo(np.float64).eps / 2
+        bound = (abs_a.t() @ y.abs()).cpu().numpy() * (k * u / (1 - k * u))
+        diff = (got - ref).abs().cpu().numpy()
+        assert np.all(diff <= 2 * bound)
+
+
+def test_noalloc_rejects_oversized_input(native):
+    _, lib = native
+    rc = lib.amfls_gpu_dense_apply_transpose_noalloc(2, (1 << 20) + 1, ctypes.c_void_p(8),
+                                                     ctypes.c_void_p(8), ctypes.c_void_p(8), None)
+    assert rc == 2
+    assert b"exceeds the fixed scratch" in lib.amfls_gpu_last_error()
