@@ -188,9 +188,13 @@ class DeviceOperator:
                     val.numel(), stream, ctypes.byref(handle)))
                 self._keep = None
             elif matrix.layout == torch.strided:
-                dense = matrix.contiguous()
+                # a column-major view (the transpose of a contiguous tensor) is
+                # used in place; anything else is made row-major contiguous
+                column_major = (not matrix.is_contiguous()) and matrix.t().is_contiguous()
+                dense = matrix if column_major else matrix.contiguous()
                 _native.check(lib.amfls_gpu_dense_operator_create(
-                    self.rows, self.cols, dense.data_ptr(), 0, stream, ctypes.byref(handle)))
+                    self.rows, self.cols, dense.data_ptr(), int(column_major), stream,
+                    ctypes.byref(handle)))
                 self._keep = dense
             else:
                 raise ValueError("matrix must use dense strided or sparse CSR storage")

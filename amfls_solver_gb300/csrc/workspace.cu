@@ -644,6 +644,25 @@ Workspace::~Workspace() {
     cudaFree(g_);
     cudaFree(qr_);
     cudaFree(qr_state_);
+    cudaFree(U2_);
+    cudaFree(BR_);
+    cudaFree(BL_);
+    cudaFree(BQ_);
+    cudaFree(BT_);
+    cudaFree(small_);
+    cudaFree(coefs_);
+    cudaFree(bpart_);
+    cudaFree(tsqr_);
+    cudaFree(dflags_);
+    cudaFree(dnorm_);
+    cudaFree(d_meta_);
+    cudaFree(d_vals_);
+    cudaFree(d_pstate_);
+    cudaFree(d_carry_);
+    cudaFree(d_pwork_);
+    cudaFree(d_y_);
+    for (cudaEvent_t e : ev_)
+        if (e) cudaEventDestroy(e);
 }
 
 void Workspace::ensure_t_capacity(int cols) {
@@ -725,16 +744,6 @@ void Workspace::initialize(const double* d_aux, int aux_cols) {
     AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
     AMFLS_CUDA(cudaStreamSynchronize(stream_));
     if (b_norm_ > 0.0 && aux_cols > 0) append_left_seed(d_aux, aux_cols);
-}
-
-int Workspace::append_left_seed(const double* d_seed, int cols) {
-    (void)d_seed;
-    if (cols <= 0) return 0;
-    throw std::runtime_error("block (width > 1) levels are not available in this build");
-}
-
-bool Workspace::block_level() {
-    throw std::runtime_error("block (width > 1) levels are not available in this build");
 }
 
 // The kernels of one width-one level.  Every per-level value (k, the
@@ -836,7 +845,7 @@ void Workspace::build_graph(int pcap) {
 
 void Workspace::advance_to(int target_depth) {
     if (!initialized_) throw std::logic_error("block Golub-Kahan workspace is not initialized");
-    if (host_.left_width + host_.pending > 1) {
+    if (block_mode_) {
         while (can_advance() && host_.depth < target_depth) {
             if (!block_level()) break;
         }
@@ -864,6 +873,8 @@ void Workspace::advance_to(int target_depth) {
 }
 
 bool Workspace::advance_level() {
+    if (!initialized_) throw std::logic_error("block Golub-Kahan workspace is not initialized");
+    if (block_mode_) return block_level();
     const int before = host_.depth;
     advance_to(host_.depth + 1);
     sync();
@@ -891,6 +902,16 @@ void Workspace::solve_projected(double* d_x) {
     projected_flags_ = 0;
     if (k == 0) {
         AMFLS_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n_, stream_));
+        return;
+    }
+    if (block_mode_) {
+        int flags = 0;
+        const double* y = block_projected_y(&flags);
+        v_c_kernel<<<(int)((n_ + 31) / 32), kThreads, 0, stream_>>>(
+            V_->device_table(), n_, k, y, nullptr, d_x, 0, partials_, counter_ + 5, dstate_,
+            kHookNone, m_, 0, 1);
+        AMFLS_LAUNCHED();
+        projected_flags_ = flags;
         return;
     }
     const double rcond = std::min(0.5, 64.0 * kEps * std::max(host_.rows_t, k));

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "device_operator.hpp"
+#include "vector_ops.hpp"
 #include "workspace_state.hpp"
 
 namespace amfls_gpu {
@@ -96,12 +97,45 @@ public:
     double* scratch_partials() const { return partials_; }
     unsigned* scratch_counter() const { return counter_; }
 
+    // true once a level or seed wider than one column has been seen
+    bool block_mode() const { return block_mode_; }
+
 private:
     void enqueue_level_kernels(cudaStream_t s, int pcap);
     void build_graph(int pcap);
     void invalidate_graph();
-    bool block_level();
     void ensure_t_capacity(int cols);
+
+    // ---- block (width > 1) levels, host-synchronised (block_level.cu) ----
+    // Result of orthogonalize_and_factor (krylov_workspace.cpp:43-52, 82-310).
+    struct Factor {
+        int rank = 0;
+        std::vector<double> coefficients;  // basis cols x block cols (when retained)
+        std::vector<double> factor;        // rank x block cols
+        double discarded = 0.0;
+        double tracked = 0.0;
+        double cutoff = 0.0;
+        bool positive_below = false;
+        bool nonfinite = false;
+    };
+    // basis: the panel-stored V (first `cols` columns) or a column-major
+    // m x cols matrix
+    struct Basis {
+        bool panels;
+        const double* mat;
+        int cols;
+    };
+    Factor orthogonalize_and_factor(double* block, int cols, const Basis& basis, int max_rank,
+                                    double scale, int tracked, bool retain, double* q_out);
+    bool block_level();
+    void enter_block_mode();
+    void ensure_block_capacity(int width);
+    void ensure_u_capacity(int cols);
+    double device_norm(const double* x, long long count);
+    double timed_apply(bool transpose, const double* in, int cols, double* out);
+    void push_state();
+    const double* block_projected_y(int* flags);  // y (k) of the record-based solve
+    void upload(double* dst, const std::vector<double>& src);
 
     const DeviceOperator& op_;
     cudaStream_t stream_;
@@ -150,6 +184,52 @@ private:
     long long counted_body_runs_ = 0;  // body runs already added to launch_count()
     long long graph_launches_ = 0;
     unsigned long long seen_a_ns_ = 0, seen_at_ns_ = 0;
+
+    // block mode state (host side; device buffers below)
+    bool block_mode_ = false;
+    int pending_requested_ = 0;
+    int pending_retained_ = 0;
+    std::vector<double> coupling_;  // frontier coupling, left_width x prev_right_width
+    // level records of T: meta (r, aw, nlw, value offset, state offset) and
+    // values G | N | g (see block.hpp)
+    std::vector<int> rec_meta_;
+    std::vector<double> rec_vals_;
+    long long rec_state_size_ = 0;
+    int rec_last_r_ = 0;
+    int rec_width_ = 1;
+    int rec_solved_ = 0;  // levels folded into the projected-solve carry
+    int* d_meta_ = nullptr;
+    long long d_meta_cap_ = 0;
+    double* d_vals_ = nullptr;
+    long long d_vals_cap_ = 0;
+    long long d_vals_uploaded_ = 0;
+    int d_meta_uploaded_ = 0;
+    double* d_pstate_ = nullptr;
+    long long d_pstate_cap_ = 0;
+    double* d_carry_ = nullptr;
+    long long d_carry_cap_ = 0;
+    double* d_pwork_ = nullptr;
+    long long d_pwork_cap_ = 0;
+    double* d_y_ = nullptr;
+    long long d_y_cap_ = 0;
+    // block scratch
+    int bcap_ = 0;             // block width the residual buffers hold
+    double* BR_ = nullptr;     // n x bcap right residual
+    double* BL_ = nullptr;     // m x bcap left residual / seed
+    double* BQ_ = nullptr;     // n x bcap new right block
+    double* BT_ = nullptr;     // max(m, n) x bcap block before re-orthogonalisation
+    double* U2_ = nullptr;     // m x ucap next left block
+    double* small_ = nullptr;  // factorisation scratch (width^2 sized)
+    long long small_cap_ = 0;
+    double* coefs_ = nullptr;  // two passes of basis^T block coefficients
+    long long coefs_cap_ = 0;
+    double* bpart_ = nullptr;  // partial sums of the tall-skinny products
+    long long bpart_cap_ = 0;
+    double* tsqr_ = nullptr;
+    long long tsqr_cap_ = 0;
+    int* dflags_ = nullptr;    // [0] nonfinite coefficients, [1] Cholesky, [2] projected
+    NormResult* dnorm_ = nullptr;
+    cudaEvent_t ev_[2] = {nullptr, nullptr};
 };
 
 }  // namespace amfls_gpu

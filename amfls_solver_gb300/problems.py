@@ -69,6 +69,12 @@ class DenseProblem:
     def cols(self) -> int:
         return int(self.matrix.shape[1])
 
+    def to_dense(self) -> np.ndarray:
+        return np.asarray(self.matrix)
+
+    def matvec(self, x: np.ndarray) -> np.ndarray:
+        return self.matrix @ x
+
 
 def _distinct_columns(rng: np.random.Generator, lengths: np.ndarray, n: int) -> np.ndarray:
     """Uniform column indices, distinct within each row, sorted within each row."""

@@ -150,6 +150,75 @@ def test_csr_solve_matches_reference(amfls, name):
         assert cert <= tol
 
 
+BLOCK_SOLVES = [n for n in SOLVE_FIXTURES if "dense" in n or "fixed" in n]
+
+
+def _matrix_tensor(prob):
+    """Dense problems keep their layout: a Fortran-ordered matrix becomes a
+    column-major CUDA view (the transpose of a contiguous tensor)."""
+    if hasattr(prob, "matrix"):
+        mat = prob.matrix
+        if mat.flags.c_contiguous:
+            return torch.from_numpy(mat).cuda()
+        return torch.from_numpy(np.ascontiguousarray(mat.T)).cuda().t()
+    return csr_tensor(prob)
+
+
+@pytest.mark.parametrize("name", BLOCK_SOLVES)
+def test_block_and_dense_solves_match_reference(amfls, name):
+    """Fixed-width RBGK (block levels from the first level) and dense AMFLS.
+
+    Fixed RBGK's widths do not depend on timings, so its counters must match
+    exactly.  Dense AMFLS's width controller weighs measured seconds (the
+    dense cost model is flat), so its counters are compared only when the
+    GPU took the same widening decisions."""
+    data, prob = load_golden(name)
+    opts = golden_options(data)
+    algorithm = opts.pop("algorithm", "amfls")
+    mat = _matrix_tensor(prob)
+    b = torch.from_numpy(prob.b).cuda()
+    fn = amfls.run_fixed_rbgk if algorithm == "fixed_rbgk" else amfls.run_amfls
+    r = fn(mat, b, **opts)
+    c = data["counters"]
+    assert (r.status, r.stop_reason) == (int(data["status"]), int(data["stop_reason"]))
+    if algorithm == "fixed_rbgk" or r.auxiliary_width == c[10]:
+        assert (r.depth, r.basis_rank, r.auxiliary_width, r.iterations) == (c[9], c[11], c[10], c[8])
+        assert (r.search_a_columns, r.search_at_columns) == (c[4], c[5])
+        np.testing.assert_array_equal(r.trace_int[:, :3].numpy(), data["trace_int"][:, :3])
+    x, xr = r.solution.cpu().numpy(), data["solution"]
+    check_solution(prob, x, xr, opts["regularization"], opts["tolerance"], r.status == 0)
+    if r.status == 0:
+        reg = opts["regularization"]
+        cert = r.relative_energy_error_upper_bound if reg > 0 else r.backward_error_upper_bound
+        assert cert <= opts["tolerance"]
+
+
+@pytest.mark.parametrize("width,lam,tol", [(4, 0.0, 1e-8), (8, 1e-4, 1e-10), (3, 1e-6, 1e-9)])
+def test_medium_fixed_rbgk_against_oracle(amfls, width, lam, tol):
+    from amfls_solver_gb300 import problems
+
+    p = problems.scaled_uniform_csr(5000, 1200, per_row=8, decades=5.0, seed=21 + width)
+    ref = orc.solve_fixed_rbgk(p, auxiliary_width=width, regularization=lam, tolerance=tol,
+                               seed=5, maximum_depth=400)
+    r = amfls.run_fixed_rbgk(csr_tensor(p), torch.from_numpy(p.b).cuda(), auxiliary_width=width,
+                             regularization=lam, tolerance=tol, seed=5, maximum_depth=400)
+    assert (r.status, r.stop_reason) == (ref["status"], ref["stop_reason"])
+    assert (r.depth, r.basis_rank) == (ref["counters"][9], ref["counters"][11])
+    assert (r.search_a_columns, r.search_at_columns) == (ref["counters"][4], ref["counters"][5])
+    check_solution(p, r.solution.cpu().numpy(), ref["solution"], lam, tol, r.status == 0)
+
+
+def test_medium_dense_against_oracle(amfls):
+    from amfls_solver_gb300 import problems
+
+    p = problems.scaled_dense(4000, 300, decades=6.0, seed=7)
+    ref = orc.solve_amfls(p, regularization=1e-6, tolerance=1e-10, seed=1)
+    r = amfls.run_amfls(_matrix_tensor(p), torch.from_numpy(p.b).cuda(), regularization=1e-6,
+                        tolerance=1e-10, seed=1)
+    assert (r.status, r.stop_reason) == (ref["status"], ref["stop_reason"])
+    check_solution(p, r.solution.cpu().numpy(), ref["solution"], 1e-6, 1e-10, r.status == 0)
+
+
 @pytest.mark.parametrize("lam,tol", [(0.0, 1e-8), (1e-4, 1e-10)])
 def test_medium_csr_against_oracle(amfls, lam, tol):
     from amfls_solver_gb300 import problems
