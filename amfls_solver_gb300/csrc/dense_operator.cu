@@ -3,11 +3,12 @@
 // Replaces DenseOperator (src/algorithms/mathematics/operators/dense_operator.cpp:20-185,
 // column-major, dgemm) and RowMajorDenseOperator
 // (row_major_dense_operator.cpp:106-258, row-major, the torch path).
-// The product along the contiguous dimension is a warp-per-output dot
-// product; the product across it keeps one output per thread (coalesced
-// over the contiguous dimension) and splits the long dimension into chunks
-// whose partial sums a second kernel adds in a fixed order, so results are
-// deterministic.  The certified norm model and the rounding-step counts
+// The product along the contiguous dimension gives each warp two outputs
+// (lanes stride the contiguous index); the product across it keeps one
+// output per thread (coalesced over the contiguous dimension).  Both split
+// the long dimension into chunks whose partial sums a second kernel adds in
+// a fixed order, so results are deterministic, and both take up to eight
+// right-hand columns per pass over A.  The certified norm model and the rounding-step counts
 // (2 cols + 2 for A, 2 rows + 2 for A^T) follow the reference; row and column
 // sums of |a_ij| are accumulated in the reference's storage order.
 // On GB300 FP64 issue rate, not HBM bandwidth, bounds these kernels
@@ -28,44 +29,88 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kTargetBlocks = 152 * 8;
 
-// out[o] = sum_i A(o, i) x(i) where o runs over the strided dimension:
-// element (o, i) at a[o * ld_o + i * ld_i] with ld_i == 1 (contiguous).
-__global__ void dot_rows_kernel(const double* __restrict__ a, long long ld, int outer, int inner,
-                                const double* __restrict__ x, double* y, const int* guard) {
+// ---- block products (s columns per pass over A, s <= 8 per launch) ----
+// Both directions split the long dimension into chunks whose partial sums
+// land in partial[(chunk * S + c) * outer + o]; reduce_block_kernel adds the
+// chunks in a fixed order.  A is read once per group of eight columns, and
+// every element read feeds S fused multiply-adds.
+constexpr int kDotOutputsPerWarp = 2;
+
+// A(o, i) at a[o * ld + i] (i contiguous): a warp owns kDotOutputsPerWarp
+// outputs and strides i across its lanes.
+template <int S>
+__global__ void __launch_bounds__(kThreads)
+dot_block_kernel(const double* __restrict__ a, long long ld, int outer, int inner, int chunk,
+                 const double* __restrict__ x, long long ldx, double* partial, const int* guard) {
+    constexpr int J = kDotOutputsPerWarp;
     if (guard && *guard == 0) return;
     const int lane = threadIdx.x & 31;
-    for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < outer;
-         w += ((long long)gridDim.x * blockDim.x) >> 5) {
-        const double* row = a + w * ld;
-        double acc = 0.0;
-        for (int i = lane; i < inner; i += 32) acc = fma(row[i], __ldg(x + i), acc);
-        acc = warp_sum(acc);
-        if (lane == 0) y[w] = acc;
+    const long long o0 = ((long long)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * J;
+    if (o0 >= outer) return;
+    const int ch = blockIdx.y;
+    const int i0 = ch * chunk, i1 = min(inner, i0 + chunk);
+    const double* rows[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) rows[j] = a + min(o0 + j, (long long)outer - 1) * ld;
+    double acc[J][S];
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+        for (int c = 0; c < S; ++c) acc[j][c] = 0.0;
+    for (int i = i0 + lane; i < i1; i += 32) {
+        double xv[S];
+#pragma unroll
+        for (int c = 0; c < S; ++c) xv[c] = __ldg(x + i + c * ldx);
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const double av = __ldg(rows[j] + i);
+#pragma unroll
+            for (int c = 0; c < S; ++c) acc[j][c] = fma(av, xv[c], acc[j][c]);
+        }
     }
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+            const double v = warp_sum(acc[j][c]);
+            if (lane == 0 && o0 + j < outer) partial[((long long)ch * S + c) * outer + o0 + j] = v;
+        }
 }
 
-// partial[c][o] = sum_{i in chunk c} A(i, o) x(i): A(i, o) at a[i * ld + o]
-__global__ void sum_cols_kernel(const double* __restrict__ a, long long ld, int outer, int inner,
-                                int chunk, const double* __restrict__ x, double* partial,
-                                const int* guard) {
+// A(i, o) at a[i * ld + o] (o contiguous): a thread owns one output.
+template <int S>
+__global__ void __launch_bounds__(kThreads)
+across_block_kernel(const double* __restrict__ a, long long ld, int outer, int inner, int chunk,
+                    const double* __restrict__ x, long long ldx, double* partial,
+                    const int* guard) {
     if (guard && *guard == 0) return;
     const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const int c = blockIdx.y;
     if (o >= outer) return;
-    const int i0 = c * chunk, i1 = min(inner, i0 + chunk);
-    double acc = 0.0;
-    for (int i = i0; i < i1; ++i) acc = fma(a[(long long)i * ld + o], __ldg(x + i), acc);
-    partial[(long long)c * outer + o] = acc;
+    const int ch = blockIdx.y;
+    const int i0 = ch * chunk, i1 = min(inner, i0 + chunk);
+    double acc[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) acc[c] = 0.0;
+    for (int i = i0; i < i1; ++i) {
+        const double av = __ldg(a + (long long)i * ld + o);
+#pragma unroll
+        for (int c = 0; c < S; ++c) acc[c] = fma(av, __ldg(x + i + c * ldx), acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < S; ++c) partial[((long long)ch * S + c) * outer + o] = acc[c];
 }
 
-__global__ void add_chunks_kernel(const double* partial, int chunks, int outer, double* y,
-                                  const int* guard) {
+__global__ void reduce_block_kernel(const double* partial, int chunks, int S, int outer,
+                                    double* y, long long ldy, const int* guard) {
     if (guard && *guard == 0) return;
-    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < outer;
-         o += (long long)gridDim.x * blockDim.x) {
+    const long long total = (long long)S * outer;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(t / outer);
+        const long long o = t % outer;
         double s = 0.0;
-        for (int c = 0; c < chunks; ++c) s += partial[(long long)c * outer + o];
-        y[o] = s;
+        for (int ch = 0; ch < chunks; ++ch) s += partial[((long long)ch * S + c) * outer + o];
+        y[o + c * ldy] = s;
     }
 }
 
@@ -222,12 +267,38 @@ int grid_1d(long long items) {
     return (int)std::max<long long>(1, std::min<long long>(kTargetBlocks, (items + 255) / 256));
 }
 
-// chunking of the long dimension for the across-contiguous product
-void split_chunks(int out_n, int in_n, int& chunks, int& chunk) {
-    const int oblocks = (out_n + 255) / 256;
-    chunks = std::max(1, std::min((kTargetBlocks + oblocks - 1) / oblocks, (in_n + 63) / 64));
+// chunking for the block kernels: enough blocks to fill the GPU twice over
+void block_chunks(bool dot, int out_n, int in_n, int& blocks_x, int& chunks, int& chunk) {
+    if (dot) {
+        const long long groups = (out_n + kDotOutputsPerWarp - 1) / kDotOutputsPerWarp;
+        blocks_x = (int)((groups + kThreads / 32 - 1) / (kThreads / 32));
+    } else {
+        blocks_x = (out_n + kThreads - 1) / kThreads;
+    }
+    const int min_rows = dot ? 256 : 32;
+    chunks = std::max(1, std::min((2 * kTargetBlocks + blocks_x - 1) / blocks_x,
+                                  (in_n + min_rows - 1) / min_rows));
     chunk = (in_n + chunks - 1) / chunks;
     chunks = (in_n + chunk - 1) / chunk;
+}
+
+template <int S>
+void launch_block(bool dot, const double* a, long long ld, int out_n, int in_n, const double* x,
+                  long long ldx, double* partial, double* y, long long ldy, cudaStream_t s,
+                  const int* guard = nullptr) {
+    int blocks_x = 0, chunks = 0, chunk = 0;
+    block_chunks(dot, out_n, in_n, blocks_x, chunks, chunk);
+    const dim3 grid(blocks_x, chunks);
+    if (dot)
+        dot_block_kernel<S><<<grid, kThreads, 0, s>>>(a, ld, out_n, in_n, chunk, x, ldx, partial,
+                                                       guard);
+    else
+        across_block_kernel<S><<<grid, kThreads, 0, s>>>(a, ld, out_n, in_n, chunk, x, ldx,
+                                                          partial, guard);
+    AMFLS_LAUNCHED();
+    reduce_block_kernel<<<grid_1d((long long)S * out_n), kThreads, 0, s>>>(partial, chunks, S,
+                                                                           out_n, y, ldy, guard);
+    AMFLS_LAUNCHED();
 }
 
 }  // namespace
@@ -249,16 +320,15 @@ DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool co
     AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * 8));
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * 8, stream));
     AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows, cols)));
-    // partial sums of the across-contiguous product, sized once so that
-    // products can be captured into CUDA graphs
-    {
-        const int out_n = column_major ? rows : cols;  // the non-dot direction
-        const int in_n = column_major ? cols : rows;
-        int chunks = 0, chunk = 0;
-        split_chunks(out_n, in_n, chunks, chunk);
-        partial_cap_ = (long long)chunks * out_n;
-        AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * std::max<long long>(1, partial_cap_)));
+    // partial sums of the chunked products, sized once so that products can
+    // be captured into CUDA graphs
+    for (int tr = 0; tr < 2; ++tr) {  // both directions, up to 8 columns per pass
+        const int on = tr ? cols : rows, inn = tr ? rows : cols;
+        int bx = 0, ch = 0, ck = 0;
+        block_chunks(column_major == (tr == 1), on, inn, bx, ch, ck);
+        partial_cap_ = std::max(partial_cap_, 8LL * ch * on);
     }
+    AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * std::max<long long>(1, partial_cap_)));
     // w: acc[5] | frob(inner) | model[2] | frob(outer) | partials (inner) | partials (outer)
     double* w = nullptr;
     const int ig = grid_1d(inner), og = grid_1d(outer);
@@ -293,44 +363,50 @@ DenseOperator::~DenseOperator() {
 
 void DenseOperator::product(bool transpose, const double* x, double* y, const int* guard,
                             cudaStream_t s) const {
-    // y has length rows (apply) or cols (transpose)
+    // y has length rows (apply) or cols (transpose).  The contiguous
+    // dimension decides the kernel: row-major rows are contiguous (apply =
+    // dot of rows); column-major columns are (transpose = dot of columns).
     const int out_n = transpose ? cols_ : rows_;
     const int in_n = transpose ? rows_ : cols_;
-    // contiguous dimension: row-major rows are contiguous (apply = dot rows);
-    // column-major columns are contiguous (transpose = dot rows of A^T)
     const bool dot = column_major_ == transpose;
     const long long ld = column_major_ ? rows_ : cols_;
-    if (dot) {
-        const long long warps = out_n;
-        const int grid = (int)std::max<long long>(1, std::min<long long>(kTargetBlocks * 2, (warps + 7) / 8));
-        dot_rows_kernel<<<grid, kThreads, 0, s>>>(a_, ld, out_n, in_n, x, y, guard);
-        AMFLS_LAUNCHED();
-    } else {
-        int chunks = 0, chunk = 0;
-        split_chunks(out_n, in_n, chunks, chunk);
-        const int oblocks = (out_n + 255) / 256;
-        if ((long long)chunks * out_n > partial_cap_)
-            throw std::logic_error("dense operator partial buffer is too small");
-        sum_cols_kernel<<<dim3(oblocks, chunks), kThreads, 0, s>>>(a_, ld, out_n, in_n, chunk, x,
-                                                                   partials_, guard);
-        AMFLS_LAUNCHED();
-        add_chunks_kernel<<<grid_1d(out_n), kThreads, 0, s>>>(partials_, chunks, out_n, y, guard);
-        AMFLS_LAUNCHED();
+    launch_block<1>(dot, a_, ld, out_n, in_n, x, in_n, partials_, y, out_n, s, guard);
+}
+
+void DenseOperator::block_product(bool transpose, const double* x, int block_cols, double* y,
+                                  cudaStream_t s) const {
+    const int out_n = transpose ? cols_ : rows_;
+    const int in_n = transpose ? rows_ : cols_;
+    const bool dot = column_major_ == transpose;
+    const long long ld = column_major_ ? rows_ : cols_;
+    for (int c0 = 0; c0 < block_cols; c0 += 8) {
+        const int sc = std::min(8, block_cols - c0);
+        const double* xs = x + (long long)c0 * in_n;
+        double* ys = y + (long long)c0 * out_n;
+        switch (sc) {
+            case 1: launch_block<1>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            case 2: launch_block<2>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            case 3: launch_block<3>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            case 4: launch_block<4>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            case 5: launch_block<5>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            case 6: launch_block<6>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            case 7: launch_block<7>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+            default: launch_block<8>(dot, a_, ld, out_n, in_n, xs, in_n, partials_, ys, out_n, s); break;
+        }
     }
-    AMFLS_LAUNCHED();
 }
 
 void DenseOperator::apply(const double* x, int block_cols, double* y, cudaStream_t s) const {
     if (x == nullptr || y == nullptr || block_cols <= 0)
         throw std::invalid_argument("dense apply block is invalid");
-    for (int c = 0; c < block_cols; ++c) product(false, x + (long long)c * cols_, y + (long long)c * rows_, nullptr, s);
+    block_product(false, x, block_cols, y, s);
 }
 
 void DenseOperator::apply_transpose(const double* y, int block_cols, double* x,
                                     cudaStream_t s) const {
     if (x == nullptr || y == nullptr || block_cols <= 0)
         throw std::invalid_argument("dense transpose block is invalid");
-    for (int c = 0; c < block_cols; ++c) product(true, y + (long long)c * rows_, x + (long long)c * cols_, nullptr, s);
+    block_product(true, y, block_cols, x, s);
 }
 
 bool DenseOperator::product1(bool transpose, const double* x, const Epilogue& ep,
@@ -352,7 +428,6 @@ void DenseOperator::apply_refined(const double* x_hi, const double* x_lo, double
                                                                x_lo, y_hi, y_lo, finite);
         AMFLS_LAUNCHED();
     }
-    AMFLS_LAUNCHED();
 }
 
 void DenseOperator::apply_transpose_refined(const double* y_hi, const double* y_lo, double* x_hi,
@@ -366,7 +441,6 @@ void DenseOperator::apply_transpose_refined(const double* y_hi, const double* y_
                                                                y_lo, x_hi, x_lo, finite);
         AMFLS_LAUNCHED();
     }
-    AMFLS_LAUNCHED();
 }
 
 }  // namespace amfls_gpu

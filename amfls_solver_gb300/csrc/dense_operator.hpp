@@ -38,6 +38,8 @@ public:
 private:
     void product(bool transpose, const double* x, double* y, const int* guard,
                  cudaStream_t s) const;
+    void block_product(bool transpose, const double* x, int block_cols, double* y,
+                       cudaStream_t s) const;
     int rows_, cols_;
     const double* a_;
     bool column_major_;

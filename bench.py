@@ -4,7 +4,10 @@
                     [--workload NAME]
 
 A step is one complete AMFLS solve to tolerance of a seeded synthetic
-problem with the workload's shape.  Prints one JSON line (rank 0).
+problem with the workload's shape.  Prints one JSON line (rank 0).  The
+default workload is the 100000 x 2000 column-major dense operator
+G diag(d) (d geometric from 1 to 1e-6, b ~ N(0,1), lambda = 1e-6,
+tol = 1e-10); --workload csr_20000x5000 runs the 20000 x 5000 CSR problem.
 
 value     mean device time of one solve with the operator and b already in
           HBM (CUDA events around the C-ABI solve call, operator built once);
@@ -13,6 +16,9 @@ e2e       the same solve through the public API run_amfls on host tensors:
           construction, solve, device->host copy of the solution;
 roofline  the dominant kernel timed live with CUDA events on its stream over
           repeated launches (algorithmic bytes per launch / mean duration);
+          for the dense operator the FP64 issue rate, not HBM, is the bound,
+          so the line also carries its FP64 rate against a cuBLAS DGEMM
+          measured in the same run;
 cpu_baseline  the oracle (the CPU restatement of the reference) on this host,
           timed on bounded depth-capped samples and extrapolated to the GPU's
           depth with a fitted t(D) = a D + b D^2 (per-level cost grows with
@@ -49,7 +55,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="csr_20000x5000")
+    ap.add_argument("--workload", default="dense_100000x2000")
     ap.add_argument("--cpu-sample", type=int, default=1, help="0 skips the cpu_baseline leg")
     return ap.parse_args()
 
@@ -129,6 +135,10 @@ def make_workload(name):
     return prob, opts
 
 
+# oracle levels per depth-capped CPU sample (the larger of the two samples)
+CPU_SAMPLE_LEVELS = {"dense_100000x2000": 240, "csr_20000x5000": 768}
+
+
 def algorithmic_bytes(prob):
     """Bytes one single-column product moves at minimum (int32 indices in HBM)."""
     if hasattr(prob, "row_offsets"):
@@ -141,32 +151,68 @@ def algorithmic_bytes(prob):
 # ------------------------------------------------------------ CPU legs ----
 
 def cpu_estimate(prob, opts, gpu_depth, budget_levels):
-    """Oracle time-to-tol estimate from two depth-capped samples."""
+    """Oracle time-to-tol estimate: operator construction timed once, then
+    three depth-capped solves on the built operator, fitted exactly by
+    t(D) = c + a D + b D^2 (b >= 0; otherwise the line through the two
+    deepest samples) and evaluated at the GPU's depth."""
     from oracle import amfls_oracle as orc
-    d2 = max(4, min(budget_levels, gpu_depth))
-    d1 = max(2, d2 // 2)
-    times = []
-    for d in (d1, d2):
+    t0 = time.perf_counter()
+    op = orc.Operator(prob)
+    t_op = time.perf_counter() - t0
+    d3 = max(6, min(budget_levels, gpu_depth))
+    ds = [max(2, d3 // 3), max(4, (2 * d3) // 3), d3]
+    ts = []
+    for d in ds:
         t0 = time.perf_counter()
-        orc.solve_amfls(prob, maximum_depth=d, **opts)
-        times.append(time.perf_counter() - t0)
-    # t(D) = a D + b D^2 through both samples
-    (t1, t2), (x1, x2) = times, (float(d1), float(d2))
-    b = max(0.0, (t2 / x2 - t1 / x1) / (x2 - x1))
-    a = max(0.0, t1 / x1 - b * x1)
+        orc.solve_amfls_operator(op, prob.b, maximum_depth=d, **opts)
+        ts.append(time.perf_counter() - t0)
+    x = np.array(ds, dtype=np.float64)
+    c, a, b = np.linalg.solve(np.stack([np.ones(3), x, x * x], axis=1), np.array(ts))
+    if b < 0.0 or a < 0.0:
+        a = (ts[2] - ts[1]) / (x[2] - x[1])
+        c, b = ts[2] - a * x[2], 0.0
     k = float(gpu_depth)
-    est = a * k + b * k * k if gpu_depth > d2 else t2
+    solve = c + a * k + b * k * k if gpu_depth > d3 else ts[2]
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": est, "unit": "s", "cores": threads, "kind": "port",
-            "sample": (f"oracle (CPU restatement) solves capped at depth {d1} and {d2} "
-                       f"({t1:.2f} s, {t2:.2f} s) on {threads} host threads, extrapolated "
-                       f"to the GPU's depth {gpu_depth} with t(D) = a D + b D^2")}
+    return {"value": t_op + solve, "unit": "s", "cores": threads, "kind": "port",
+            "sample": (f"oracle (CPU restatement; dense products through the host BLAS) on "
+                       f"{threads} host threads: operator construction {t_op:.2f} s, solves "
+                       f"capped at depth {ds[0]}, {ds[1]}, {ds[2]} ({ts[0]:.2f}, {ts[1]:.2f}, "
+                       f"{ts[2]:.2f} s) fitted by c + a D + b D^2 and evaluated at the "
+                       f"GPU's depth {gpu_depth}")}
+
+
+def fp64_dgemm_tflops(dev, stream):
+    """cuBLAS DGEMM rate on this GPU (best of 3), the FP64 denominator."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        torch.matmul(a, b)
+        e1.record(stream)
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+# DRAM bytes (read + write) per launch of the dominant kernel from one ncu
+# capture of the same workload (profiles/dense_block_product_100000x2000_full.md:
+# mean of the A v and A^T u launches), or None when no capture covers it
+TRAFFIC = {"dense_100000x2000": 0.5 * ((1.600079e9 + 7.885824e6) + (1.604726e9 + 3.578112e6))}
 
 
 # --------------------------------------------------------------- arms ----
 
 # depth of the full solve on each workload (bench seed 20251203)
-KNOWN_DEPTH = {"csr_20000x5000": 3797}
+# (the dense workload never meets its tolerance before the basis fills the
+# 2000 columns, on the reference and on this solver alike)
+KNOWN_DEPTH = {"csr_20000x5000": 3797, "dense_100000x2000": 2000}
 
 def run_reference(args, world, rank):
     if rank != 0:
@@ -178,7 +224,7 @@ def run_reference(args, world, rank):
         KNOWN_DEPTH.get(args.workload, 4096)
     vals = []
     for i in range(args.warmup + args.steps):
-        est = cpu_estimate(prob, opts, depth_hint, 768)
+        est = cpu_estimate(prob, opts, depth_hint, CPU_SAMPLE_LEVELS.get(args.workload, 512))
         if i >= args.warmup:
             vals.append(est)
     v = statistics.mean(e["value"] for e in vals)
@@ -213,8 +259,13 @@ def run_ours(args, world, rank, local):
         mat_dev = torch.sparse_csr_tensor(host["crow"], host["col"], host["val"],
                                           size=(prob.rows, prob.cols)).to(dev)
     else:
-        host = dict(mat=torch.from_numpy(np.ascontiguousarray(prob.matrix)).pin_memory())
-        mat_dev = host["mat"].to(dev)
+        # column-major workloads travel as the row-major buffer of A^T and
+        # are used on the device as the transposed (column-major) view
+        col_major = not prob.matrix.flags.c_contiguous
+        buf = np.ascontiguousarray(prob.matrix.T if col_major else prob.matrix)
+        host = dict(mat=torch.from_numpy(buf).pin_memory())
+        as_matrix = (lambda t: t.t()) if col_major else (lambda t: t)
+        mat_dev = as_matrix(host["mat"].to(dev))
     b_host = torch.from_numpy(prob.b).pin_memory()
     b_dev = b_host.to(dev)
     op = amfls.DeviceOperator(mat_dev)
@@ -278,7 +329,7 @@ def run_ours(args, world, rank, local):
                                         host["val"].to(dev, non_blocking=True),
                                         size=(prob.rows, prob.cols))
         else:
-            a = host["mat"].to(dev, non_blocking=True)
+            a = as_matrix(host["mat"].to(dev, non_blocking=True))
         bb = b_host.to(dev, non_blocking=True)
         r = amfls.run_amfls(a, bb, **{k: v for k, v in opts.items()})
         sol = r.solution.cpu()
@@ -288,39 +339,61 @@ def run_ours(args, world, rank, local):
         del a, bb, sol
     e2e = statistics.mean(e2e_times)
 
-    # dominant-kernel roofline: the operator product, timed live
+    # dominant-kernel roofline: the operator products (A v and A^T u
+    # alternate in every level), timed live on the launching stream
     vec = torch.randn(prob.cols, dtype=torch.float64, device=dev)
-    for _ in range(5):
-        op.apply(vec)
-    reps = 50
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        op.apply(vec)
-    e1.record(stream)
-    e1.synchronize()
-    kt = e0.elapsed_time(e1) * 1e-3 / reps
+    uvec = torch.randn(prob.rows, dtype=torch.float64, device=dev)
+
+    def timed(fn, reps=40):
+        for _ in range(5):
+            fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps
+
+    kt_a = timed(lambda: op.apply(vec))
+    kt_at = timed(lambda: op.apply(uvec, transpose=True))
+    kt = 0.5 * (kt_a + kt_at)
     peak, peak_kind = measured_peaks()
-    achieved = algorithmic_bytes(prob) / kt / 1e9
-    roof = {"kernel": "spmv_binned_kernel" if is_csr else "dense_operator_product",
+    nbytes = algorithmic_bytes(prob)
+    achieved = nbytes / kt / 1e9
+    roof = {"kernel": ("spmv_binned_kernel" if is_csr else
+                       "dot_block_kernel<1> (A^T u) / across_block_kernel<1> (A v)"),
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-            "launch_us": kt * 1e6, "algorithmic_bytes": algorithmic_bytes(prob)}
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": TRAFFIC.get(args.workload),
+            "launch_us": {"apply": kt_a * 1e6, "apply_transpose": kt_at * 1e6},
+            "algorithmic_bytes": nbytes}
+    if not is_csr:
+        flops = 2.0 * prob.rows * prob.cols
+        roof["fp64"] = {"achieved_tflops": flops / kt / 1e12,
+                        "dgemm_tflops": fp64_dgemm_tflops(dev, stream),
+                        "note": "FP64 issue-bound: 2 flops per 8-byte element against "
+                                "the FP64 ridge; dgemm_tflops is cuBLAS DGEMM 4096^3 "
+                                "measured in this run"}
+        roof["fp64"]["frac"] = roof["fp64"]["achieved_tflops"] / roof["fp64"]["dgemm_tflops"]
 
     if rank != 0:
         return
     cpu = None
     if args.cpu_sample and world == 1:
-        cpu = cpu_estimate(prob, opts, depth, int(os.environ.get("AMFLS_BENCH_CPU_LEVELS", "768")))
+        levels = int(os.environ.get("AMFLS_BENCH_CPU_LEVELS", "0")) or \
+            CPU_SAMPLE_LEVELS.get(args.workload, 512)
+        cpu = cpu_estimate(prob, opts, depth, levels)
     line = {"metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded numpy generator)",
             "config": {"workload": args.workload, "rows": prob.rows, "cols": prob.cols,
                        "nnz": prob.nnz if is_csr else prob.rows * prob.cols, **opts,
-                       "l2": "every solve re-reads the matrix and rebuilds the basis; "
-                             "matrix + basis exceed L2 after the first levels",
+                       "l2": "inputs larger than L2: every product re-reads the matrix "
+                             "(CSR arrays or the 1.6 GB dense matrix) and every level "
+                             "sweeps the basis; each solve rebuilds the basis from scratch",
                        "depth": depth, "status": list(status), "parallelism": "replicas"},
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

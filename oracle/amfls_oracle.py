@@ -152,7 +152,24 @@ class Operator:
         m = self._model
         return m.norm_upper, m.norm_lower, m.apply_steps, m.transpose_steps
 
+    def _dense_product(self, v, transpose):
+        """The reference's BLAS calls: column-major DenseOperator always uses
+        dgemm (dense_operator.cpp:165-185); RowMajorDenseOperator uses dgemv
+        for one column and dgemm otherwise on the transposed (n x m
+        column-major) view of its buffer (row_major_dense_operator.cpp:183-260)."""
+        a = self._keep[0]
+        v = np.asfortranarray(v.reshape(v.shape[0], -1), dtype=np.float64)
+        if self.kind == 2:  # a is m x n Fortran-ordered
+            return sblas.dgemm(1.0, a, v, trans_a=1 if transpose else 0)
+        at = a.T  # n x m Fortran-ordered view of the row-major buffer
+        if v.shape[1] == 1:
+            out = sblas.dgemv(1.0, at, v[:, 0], trans=0 if transpose else 1)
+            return np.asfortranarray(out.reshape(-1, 1))
+        return sblas.dgemm(1.0, at, v, trans_a=0 if transpose else 1)
+
     def apply(self, x):
+        if self.kind != 0:
+            return self._dense_product(np.asarray(x, dtype=np.float64), False)
         x = np.asfortranarray(x, dtype=np.float64)
         s = 1 if x.ndim == 1 else x.shape[1]
         y = np.zeros((self.rows, s), order="F")
@@ -160,6 +177,8 @@ class Operator:
         return y
 
     def apply_transpose(self, y):
+        if self.kind != 0:
+            return self._dense_product(np.asarray(y, dtype=np.float64), True)
         y = np.asfortranarray(y, dtype=np.float64)
         s = 1 if y.ndim == 1 else y.shape[1]
         x = np.zeros((self.cols, s), order="F")

@@ -123,6 +123,28 @@ def test_dense_model_matches_reference(amfls, name):
         np.abs(prob.matrix.T) @ np.abs(yy))
 
 
+@pytest.mark.parametrize("layout", ["row", "col"])
+@pytest.mark.parametrize("s", [1, 2, 3, 8, 11])
+def test_dense_block_products(amfls, layout, s):
+    """Block products read A once per eight columns; each column must equal a
+    plain float64 product to rounding (|error| <= gamma_{n+2} |A| |x|)."""
+    rng = np.random.default_rng(s)
+    m, n = 3001, 517
+    a = rng.standard_normal((m, n))
+    t = torch.from_numpy(a).cuda() if layout == "row" else \
+        torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t()
+    op = amfls.DeviceOperator(t)
+    x = rng.standard_normal((n, s))
+    y = rng.standard_normal((m, s))
+    ax = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+    aty = op.apply(torch.from_numpy(y).cuda(), transpose=True).cpu().numpy()
+    for got, ref, bound, k in [(ax, a @ x, np.abs(a) @ np.abs(x), n),
+                               (aty, a.T @ y, np.abs(a.T) @ np.abs(y), m)]:
+        g = (k + 2) * EPS
+        assert got.shape == ref.shape
+        assert np.all(np.abs(got - ref) <= 2 * g * bound)
+
+
 CSR_SOLVES = [n for n in SOLVE_FIXTURES if "dense" not in n and "fixed" not in n]
 
 

@@ -78,10 +78,11 @@ def test_oracle_solve_matches_reference(name):
     scale = max(np.linalg.norm(xr), 1e-300)
     assert np.linalg.norm(x - xr) <= 1e-9 * scale
     # Certified bounds.  The oracle's CSR products repeat the reference's FMA
-    # order exactly, so CSR bounds agree to rounding.  Dense products use a
-    # different summation order than BLAS; near convergence ||A^T r|| sits at
-    # its rounding floor and the bounds built from it agree only roughly.
-    rel = 1e-6 if int(data["kind"]) == 0 else 0.1
+    # order exactly and its dense products make the reference's BLAS calls
+    # (same OpenBLAS here), so the bounds agree to rounding.  On another BLAS
+    # build the dense bounds near convergence would sit at a different
+    # rounding floor.
+    rel = 1e-6
     for idx in (8, 9, 10, 13):
         a, b = r["metrics"][idx], data["metrics"][idx]
         if np.isfinite(b):
