@@ -175,6 +175,36 @@ struct BinTable {
     int row_start[7];         // rows of bin b in perm: [rs[b], rs[b+1])
 };
 
+// One lane's share of a row: elements first + g t for t = 0, 1, ...,
+// accumulated in that order.  Four elements' values and indices are loaded
+// before their gathers so that each lane keeps several independent loads in
+// flight; the streamed arrays bypass L1 and are marked evict-first so that
+// the gathered vector stays in L2.
+__device__ __forceinline__ double row_dot(const long long* __restrict__ off,
+                                          const int* __restrict__ idx,
+                                          const double* __restrict__ val,
+                                          const double* __restrict__ x, int row, int first,
+                                          int g) {
+    const long long end = off[row + 1];
+    double acc = 0.0;
+    for (long long e = off[row] + first; e < end; e += 4 * g) {
+        double v[4], xv[4];
+        int j[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const bool in = e + u * g < end;
+            v[u] = in ? __ldcs(val + e + u * g) : 0.0;
+            j[u] = in ? __ldcs(idx + e + u * g) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xv[u] = j[u] >= 0 ? __ldg(x + j[u]) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (j[u] >= 0) acc = fma(v[u], xv[u], acc);
+    }
+    return acc;
+}
+
 __global__ void __launch_bounds__(kThreads)
 spmv_binned_kernel(const long long* __restrict__ off, const int* __restrict__ idx,
                    const double* __restrict__ val, const int* __restrict__ perm, BinTable bt,
@@ -195,11 +225,7 @@ spmv_binned_kernel(const long long* __restrict__ off, const int* __restrict__ id
         const bool active = local < (long long)(bt.row_start[b + 1] - bt.row_start[b]);
         const int row = active ? perm[bt.row_start[b] + local] : 0;
         double acc = 0.0;
-        if (active) {
-            const long long end = off[row + 1];
-            for (long long e = off[row] + (lane & (g - 1)); e < end; e += g)
-                acc = fma(val[e], __ldg(&x[idx[e]]), acc);
-        }
+        if (active) acc = row_dot(off, idx, val, x, row, lane & (g - 1), g);
         for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (active && (lane & (g - 1)) == 0)
             epilogue_row(ep, row, acc, sq_t, sq_out, dot, mx_t, mx_out, nonfin);
@@ -231,9 +257,25 @@ spmm_binned_kernel(const long long* __restrict__ off, const int* __restrict__ id
         for (int c = 0; c < C; ++c) acc[c] = 0.0;
         if (active) {
             const long long end = off[row + 1];
-            for (long long e = off[row] + (lane & (g - 1)); e < end; e += g) {
-                const double a = val[e];
-                const int j = idx[e];
+            long long e = off[row] + (lane & (g - 1));
+            for (; e + g < end; e += 2 * g) {
+                const double a0 = __ldcs(val + e), a1 = __ldcs(val + e + g);
+                const int j0 = __ldcs(idx + e), j1 = __ldcs(idx + e + g);
+                double x0[C], x1[C];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    x0[c] = c < ncols ? __ldg(&x[j0 + c * ldx]) : 0.0;
+                    x1[c] = c < ncols ? __ldg(&x[j1 + c * ldx]) : 0.0;
+                }
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    acc[c] = fma(a0, x0[c], acc[c]);
+                    acc[c] = fma(a1, x1[c], acc[c]);
+                }
+            }
+            for (; e < end; e += g) {
+                const double a = __ldcs(val + e);
+                const int j = __ldcs(idx + e);
 #pragma unroll
                 for (int c = 0; c < C; ++c)
                     if (c < ncols) acc[c] = fma(a, __ldg(&x[j + c * ldx]), acc[c]);

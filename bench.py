@@ -14,6 +14,8 @@ value     mean device time of one solve with the operator and b already in
 e2e       the same solve through the public API run_amfls on host tensors:
           host->device copy of the CSR arrays / dense matrix and b, operator
           construction, solve, device->host copy of the solution;
+spmm      CSR SpMM and SpMM^T GB/s (s = 1 and 8) on the 2,000,000 x 500,000
+          power-law matrix, the metric's second half;
 roofline  the dominant kernel timed live with CUDA events on its stream over
           repeated launches (algorithmic bytes per launch / mean duration);
           for the dense operator the FP64 issue rate, not HBM, is the bound,
@@ -57,6 +59,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="dense_100000x2000")
     ap.add_argument("--cpu-sample", type=int, default=1, help="0 skips the cpu_baseline leg")
+    ap.add_argument("--spmm", type=int, default=1,
+                    help="0 skips the CSR SpMM GB/s measurement on the 2M x 500k matrix")
     return ap.parse_args()
 
 
@@ -205,6 +209,57 @@ def fp64_dgemm_tflops(dev, stream):
 # capture of the same workload (profiles/dense_block_product_100000x2000_full.md:
 # mean of the A v and A^T u launches), or None when no capture covers it
 TRAFFIC = {"dense_100000x2000": 0.5 * ((1.600079e9 + 7.885824e6) + (1.604726e9 + 3.578112e6))}
+
+
+SPMM_WORKLOAD = "csr_2000000x500000"
+
+
+def spmm_measurement(dev, stream, peak):
+    """CSR SpMM / SpMM^T HBM GB/s on the 2,000,000 x 500,000 power-law matrix
+    (40.2M nonzeros), s = 1 and s = 8 columns, through the C ABI on
+    preallocated column-major device blocks (CUDA events on the stream).
+    Algorithmic bytes: nnz (8 + 4) + (rows + 1) 4 + s (m + n) 8."""
+    import ctypes
+    import torch
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import _native, problems
+
+    prob, _ = problems.make(SPMM_WORKLOAD, seed=20251203)
+    a = torch.sparse_csr_tensor(torch.from_numpy(prob.row_offsets),
+                                torch.from_numpy(prob.column_indices),
+                                torch.from_numpy(prob.values),
+                                size=(prob.rows, prob.cols)).to(dev)
+    op = amfls.DeviceOperator(a)
+    lib = _native.load()
+    m, n, nnz = prob.rows, prob.cols, prob.nnz
+    out = {"workload": SPMM_WORKLOAD, "rows": m, "cols": n, "nnz": nnz, "peak_gbs": peak,
+           "unit": "GB/s"}
+    for cols in (1, 8):
+        x = torch.randn(cols * n, dtype=torch.float64, device=dev)
+        y = torch.randn(cols * m, dtype=torch.float64, device=dev)
+        res = {}
+        for name, fn, src, dst, rows_out in (
+                ("apply", lib.amfls_gpu_operator_apply, x, y, m),
+                ("apply_transpose", lib.amfls_gpu_operator_apply_transpose, y, x, n)):
+            def call():
+                _native.check(fn(op.handle, ctypes.c_void_p(src.data_ptr()), cols,
+                                 ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(stream.cuda_stream)))
+            for _ in range(5):
+                call()
+            reps = 30
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                call()
+            e1.record(stream)
+            e1.synchronize()
+            t = e0.elapsed_time(e1) * 1e-3 / reps
+            nbytes = nnz * 12 + (rows_out + 1) * 4 + cols * (m + n) * 8
+            res[name] = {"us": t * 1e6, "achieved": nbytes / t / 1e9,
+                         "frac": nbytes / t / 1e9 / peak, "algorithmic_bytes": nbytes}
+        out[f"s{cols}"] = res
+    return out
 
 
 # --------------------------------------------------------------- arms ----
@@ -378,6 +433,8 @@ def run_ours(args, world, rank, local):
                                 "measured in this run"}
         roof["fp64"]["frac"] = roof["fp64"]["achieved_tflops"] / roof["fp64"]["dgemm_tflops"]
 
+    spmm = spmm_measurement(dev, stream, peak) if args.spmm else None
+
     if rank != 0:
         return
     cpu = None
@@ -397,7 +454,7 @@ def run_ours(args, world, rank, local):
                        "depth": depth, "status": list(status), "parallelism": "replicas"},
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks.summary(),
+            "roofline": roof, "spmm": spmm, "cpu_baseline": cpu, "clocks": clocks.summary(),
             "gpu_launches": launches * args.steps}
     print(json.dumps(line), flush=True)
 
