@@ -7,13 +7,15 @@
 //     row, finite values; ||A|| <= min(sqrt(||A||_1 ||A||_inf), ||A||_F),
 //     ||A|| >= max(max|a_ij|, max row/column 2-norm); rounding steps
 //     2*max_row_nnz+2 and 2*max_col_nnz+2) runs as device kernels;
-//   * apply runs a row-length-binned sub-warp SpMV: rows are grouped by
-//     length and each row gets G in {1,..,32} lanes that read its nonzeros
-//     contiguously and combine by a fixed butterfly, so results are
-//     deterministic for a given matrix;
+//   * apply streams nnz-balanced tiles of rows through shared memory with
+//     bulk copies and sums each row by a merge-path segmented reduction
+//     (csr_tiles.cuh); sums are taken in an order fixed by the tiling, so
+//     results are deterministic for a given matrix;
 //   * apply_transpose does NOT scatter: it runs the same gather kernel on a
 //     transpose (CSR of A^T) built once on the device with a stable sort, so
-//     each column sums its entries in row order like the reference's scatter.
+//     each column sums its entries in row order like the reference's scatter;
+//   * the double-double validation products use a row-length-binned
+//     sub-warp kernel (rows grouped by length, G in {1,..,32} lanes a row).
 // Row and column sums of |a_ij| for the norm model are accumulated
 // sequentially in the reference's order (rows in CSR order, columns in row
 // order), so those stored sums match the reference bit for bit.
@@ -28,6 +30,7 @@
 
 #include "common.cuh"
 #include "csr_operator.hpp"
+#include "csr_tiles.cuh"
 #include "dd.cuh"
 #include "epilogue.cuh"
 #include "fp_bounds.cuh"
@@ -175,121 +178,10 @@ struct BinTable {
     int row_start[7];         // rows of bin b in perm: [rs[b], rs[b+1])
 };
 
-// One lane's share of a row: elements first + g t for t = 0, 1, ...,
-// accumulated in that order.  Four elements' values and indices are loaded
-// before their gathers so that each lane keeps several independent loads in
-// flight; the streamed arrays bypass L1 and are marked evict-first so that
-// the gathered vector stays in L2.
-__device__ __forceinline__ double row_dot(const long long* __restrict__ off,
-                                          const int* __restrict__ idx,
-                                          const double* __restrict__ val,
-                                          const double* __restrict__ x, int row, int first,
-                                          int g) {
-    const long long end = off[row + 1];
-    double acc = 0.0;
-    for (long long e = off[row] + first; e < end; e += 4 * g) {
-        double v[4], xv[4];
-        int j[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const bool in = e + u * g < end;
-            v[u] = in ? __ldcs(val + e + u * g) : 0.0;
-            j[u] = in ? __ldcs(idx + e + u * g) : -1;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) xv[u] = j[u] >= 0 ? __ldg(x + j[u]) : 0.0;
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (j[u] >= 0) acc = fma(v[u], xv[u], acc);
-    }
-    return acc;
-}
-
-__global__ void __launch_bounds__(kThreads)
-spmv_binned_kernel(const long long* __restrict__ off, const int* __restrict__ idx,
-                   const double* __restrict__ val, const int* __restrict__ perm, BinTable bt,
-                   const double* __restrict__ x, Epilogue ep, double* partials,
-                   unsigned* counter) {
-    if (ep.guard && *ep.guard == 0) return;
-    const int lane = threadIdx.x & 31;
-    double sq_t = 0.0, sq_out = 0.0, dot = 0.0, mx_t = 0.0, mx_out = 0.0;
-    int nonfin = 0;
-    const long long total = bt.warp_start[6];
-    for (long long wt = (long long)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); wt < total;
-         wt += (long long)gridDim.x * kWarpsPerBlock) {
-        int b = 0;
-#pragma unroll
-        for (int i = 1; i < 6; ++i) b += wt >= bt.warp_start[i] ? 1 : 0;
-        const int g = 1 << b;
-        const long long local = (wt - bt.warp_start[b]) * (32 >> b) + (lane >> b);
-        const bool active = local < (long long)(bt.row_start[b + 1] - bt.row_start[b]);
-        const int row = active ? perm[bt.row_start[b] + local] : 0;
-        double acc = 0.0;
-        if (active) acc = row_dot(off, idx, val, x, row, lane & (g - 1), g);
-        for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (active && (lane & (g - 1)) == 0)
-            epilogue_row(ep, row, acc, sq_t, sq_out, dot, mx_t, mx_out, nonfin);
-    }
-    finish_reduction(ep, sq_t, sq_out, dot, mx_t, mx_out, nonfin, partials, counter);
-}
-
-// Several right-hand sides: lanes share each nonzero across a chunk of up to
-// 8 columns of a column-major block (x stride ldx, y stride ldy).
-template <int C>
-__global__ void __launch_bounds__(kThreads)
-spmm_binned_kernel(const long long* __restrict__ off, const int* __restrict__ idx,
-                   const double* __restrict__ val, const int* __restrict__ perm, BinTable bt,
-                   const double* __restrict__ x, long long ldx, double* __restrict__ y,
-                   long long ldy, int ncols) {
-    const int lane = threadIdx.x & 31;
-    const long long total = bt.warp_start[6];
-    for (long long wt = (long long)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); wt < total;
-         wt += (long long)gridDim.x * kWarpsPerBlock) {
-        int b = 0;
-#pragma unroll
-        for (int i = 1; i < 6; ++i) b += wt >= bt.warp_start[i] ? 1 : 0;
-        const int g = 1 << b;
-        const long long local = (wt - bt.warp_start[b]) * (32 >> b) + (lane >> b);
-        const bool active = local < (long long)(bt.row_start[b + 1] - bt.row_start[b]);
-        const int row = active ? perm[bt.row_start[b] + local] : 0;
-        double acc[C];
-#pragma unroll
-        for (int c = 0; c < C; ++c) acc[c] = 0.0;
-        if (active) {
-            const long long end = off[row + 1];
-            long long e = off[row] + (lane & (g - 1));
-            for (; e + g < end; e += 2 * g) {
-                const double a0 = __ldcs(val + e), a1 = __ldcs(val + e + g);
-                const int j0 = __ldcs(idx + e), j1 = __ldcs(idx + e + g);
-                double x0[C], x1[C];
-#pragma unroll
-                for (int c = 0; c < C; ++c) {
-                    x0[c] = c < ncols ? __ldg(&x[j0 + c * ldx]) : 0.0;
-                    x1[c] = c < ncols ? __ldg(&x[j1 + c * ldx]) : 0.0;
-                }
-#pragma unroll
-                for (int c = 0; c < C; ++c) {
-                    acc[c] = fma(a0, x0[c], acc[c]);
-                    acc[c] = fma(a1, x1[c], acc[c]);
-                }
-            }
-            for (; e < end; e += g) {
-                const double a = __ldcs(val + e);
-                const int j = __ldcs(idx + e);
-#pragma unroll
-                for (int c = 0; c < C; ++c)
-                    if (c < ncols) acc[c] = fma(a, __ldg(&x[j + c * ldx]), acc[c]);
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < C; ++c)
-            for (int o = g >> 1; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-        if (active && (lane & (g - 1)) == 0) {
-#pragma unroll
-            for (int c = 0; c < C; ++c)
-                if (c < ncols) y[row + c * ldy] = acc[c];
-        }
-    }
+__global__ void narrow_offsets_kernel(const long long* off, int count, int* off32) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r <= count;
+         r += (long long)gridDim.x * blockDim.x)
+        off32[r] = (int)off[r];
 }
 
 // Double-double product for the validation refinement.
@@ -337,13 +229,149 @@ int setup_grid(long long items) {
 
 }  // namespace
 
+namespace {
+
+// Elements of the value / index / offset copies: n rounded up to a multiple
+// of 4 plus 4 (16-byte aligned ends; the tails are zero).
+long long padded(long long n) { return ((n + 3) & ~3LL) + 4; }
+
+// One tiling of one side (see csr_tiles.cuh), owned by the operator.
+struct TileStore {
+    int4* tiles = nullptr;
+    int* split = nullptr;
+    int2* long_rows = nullptr;
+    unsigned* long_count = nullptr;
+    double* long_part = nullptr;
+    int ntiles = 0;
+    int grid = 1;
+
+    csr_tiles::Table view() const {
+        csr_tiles::Table t;
+        t.tiles = tiles;
+        t.split = split;
+        t.long_rows = long_rows;
+        t.long_count = long_count;
+        t.long_part = long_part;
+        t.ntiles = ntiles;
+        return t;
+    }
+    void release() {
+        cudaFree(tiles);
+        cudaFree(split);
+        cudaFree(long_rows);
+        cudaFree(long_count);
+        cudaFree(long_part);
+        *this = TileStore{};
+    }
+};
+
+// Greedy cut of rows [0, count) with host offsets `off` into row blocks of at
+// most E nonzeros and E rows, and E-element slices of longer rows.
+void make_tiles(const std::vector<long long>& off, int count, int E, int C, TileStore& ts,
+                cudaStream_t stream) {
+    std::vector<int4> tiles;
+    std::vector<int> split;
+    std::vector<int2> long_rows;
+    int r = 0;
+    while (r < count) {
+        const long long len = off[r + 1] - off[r];
+        if (len > E) {
+            const int first = (int)tiles.size();
+            for (long long e = off[r]; e < off[r + 1]; e += E) {
+                tiles.push_back(make_int4(r, r + 1, (int)e, (int)std::min(e + E, off[r + 1])));
+                split.push_back((int)long_rows.size());
+            }
+            long_rows.push_back(make_int2(first, (int)tiles.size() - first));
+            ++r;
+            continue;
+        }
+        const int r0 = r;
+        const long long e0 = off[r];
+        while (r < count && off[r + 1] - e0 <= E && r - r0 < E) ++r;
+        tiles.push_back(make_int4(r0, r, (int)e0, (int)off[r]));
+        split.push_back(-1);
+    }
+    ts.ntiles = (int)tiles.size();
+    const size_t nt = std::max<size_t>(1, tiles.size()), nl = std::max<size_t>(1, long_rows.size());
+    AMFLS_CUDA(cudaMalloc(&ts.tiles, sizeof(int4) * nt));
+    AMFLS_CUDA(cudaMalloc(&ts.split, sizeof(int) * nt));
+    AMFLS_CUDA(cudaMalloc(&ts.long_rows, sizeof(int2) * nl));
+    AMFLS_CUDA(cudaMalloc(&ts.long_count, sizeof(unsigned) * nl));
+    AMFLS_CUDA(cudaMalloc(&ts.long_part, sizeof(double) * C * nt));
+    AMFLS_CUDA(cudaMemsetAsync(ts.long_count, 0, sizeof(unsigned) * nl, stream));
+    if (!tiles.empty()) {
+        AMFLS_CUDA(cudaMemcpyAsync(ts.tiles, tiles.data(), sizeof(int4) * tiles.size(),
+                                   cudaMemcpyHostToDevice, stream));
+        AMFLS_CUDA(cudaMemcpyAsync(ts.split, split.data(), sizeof(int) * split.size(),
+                                   cudaMemcpyHostToDevice, stream));
+    }
+    if (!long_rows.empty())
+        AMFLS_CUDA(cudaMemcpyAsync(ts.long_rows, long_rows.data(),
+                                   sizeof(int2) * long_rows.size(), cudaMemcpyHostToDevice,
+                                   stream));
+    AMFLS_CUDA(cudaStreamSynchronize(stream));  // host vectors go out of scope
+}
+
+// Column-major block (rows x ncols, leading dimension ld) -> row-major
+// rows x C, zero-padded beyond ncols.
+template <int C>
+__global__ void rows_major_kernel(const double* __restrict__ x, long long ld, int rows, int ncols,
+                                  double* __restrict__ xr) {
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < rows;
+         j += (long long)gridDim.x * blockDim.x) {
+        double v[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) v[c] = c < ncols ? x[j + c * ld] : 0.0;
+        double2* dst = reinterpret_cast<double2*>(xr + j * C);
+#pragma unroll
+        for (int h = 0; h < C / 2; ++h) dst[h] = make_double2(v[2 * h], v[2 * h + 1]);
+    }
+}
+
+// Resident CTAs for a tile kernel (every warp of the grid walks its own
+// tiles), at most one warp per tile and at most kMaxBlocks CTAs.
+template <int C, int E, bool kFused>
+int tile_grid(int ntiles) {
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0) {
+        constexpr int bytes = csr_tiles::smem_bytes<C, E>();
+        AMFLS_CUDA(cudaFuncSetAttribute(csr_tiles::tile_product_kernel<C, E, kFused>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        int dev = 0, nb = 0;
+        AMFLS_CUDA(cudaGetDevice(&dev));
+        AMFLS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, csr_tiles::tile_product_kernel<C, E, kFused>, csr_tiles::kThreads, bytes));
+        per_sm = std::max(1, nb);
+    }
+    const int need = (ntiles + csr_tiles::kWarps - 1) / csr_tiles::kWarps;
+    return std::max(1, std::min({need, per_sm * sms, kMaxBlocks}));
+}
+
+template <int C, bool kFused>
+void launch_tiles(const int* off, const int* idx, const double* val, const TileStore& ts,
+                  const double* x, double* y, long long ldy, int ncols, const Epilogue& ep,
+                  double* partials, unsigned* counter, cudaStream_t stream) {
+    constexpr int E = C == 1 ? csr_tiles::kE1 : csr_tiles::kEC;
+    const int grid = tile_grid<C, E, kFused>(ts.ntiles);
+    csr_tiles::tile_product_kernel<C, E, kFused>
+        <<<grid, csr_tiles::kThreads, csr_tiles::smem_bytes<C, E>(), stream>>>(
+            off, idx, val, ts.view(), x, y, ldy, ncols, ep, partials, counter);
+    AMFLS_LAUNCHED();
+}
+
+}  // namespace
+
 struct CsrOperator::Side {
     long long* off = nullptr;  // count+1
-    int* idx = nullptr;        // nnz
-    double* val = nullptr;     // nnz
-    int* perm = nullptr;       // count (rows sorted by bin)
+    int* off32 = nullptr;      // count+1, padded (bulk-copy source)
+    int* idx = nullptr;        // nnz, padded
+    double* val = nullptr;     // nnz, padded
+    int* perm = nullptr;       // count (rows sorted by bin, double-double products)
     BinTable bins{};
     int count = 0;
+    TileStore one;             // tiles of kE1 elements: single-column products
+    TileStore many;            // tiles of kEC elements: 2..8 columns
 };
 
 CsrOperator::CsrOperator(int rows, int cols, const long long* d_offsets,
@@ -375,13 +403,19 @@ void CsrOperator::release() {
         cudaFree(s->idx);
         cudaFree(s->val);
         cudaFree(s->perm);
+        cudaFree(s->off32);
         s->off = nullptr;
         s->idx = nullptr;
         s->val = nullptr;
         s->perm = nullptr;
+        s->off32 = nullptr;
+        s->one.release();
+        s->many.release();
     }
     cudaFree(scratch_);
     scratch_ = nullptr;
+    cudaFree(xrows_);
+    xrows_ = nullptr;
 }
 
 void CsrOperator::build_bins(Side& s, const int* d_bins, cudaStream_t stream) {
@@ -436,11 +470,19 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
                                            sizeof(double) * (6 * kMaxBlocks + 64));
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
     AMFLS_CUDA(cudaMalloc(&A.off, sizeof(long long) * (rows_ + 1)));
-    AMFLS_CUDA(cudaMalloc(&A.idx, sizeof(int) * std::max<long long>(1, nnz)));
-    AMFLS_CUDA(cudaMalloc(&A.val, sizeof(double) * std::max<long long>(1, nnz)));
+    AMFLS_CUDA(cudaMalloc(&xrows_, sizeof(double) * 8 * (size_t)std::max(rows_, cols_)));
+    const long long np = padded(nnz);
+    AMFLS_CUDA(cudaMalloc(&A.idx, sizeof(int) * np));
+    AMFLS_CUDA(cudaMalloc(&A.val, sizeof(double) * np));
     AMFLS_CUDA(cudaMalloc(&T.off, sizeof(long long) * (cols_ + 1)));
-    AMFLS_CUDA(cudaMalloc(&T.idx, sizeof(int) * std::max<long long>(1, nnz)));
-    AMFLS_CUDA(cudaMalloc(&T.val, sizeof(double) * std::max<long long>(1, nnz)));
+    AMFLS_CUDA(cudaMalloc(&T.idx, sizeof(int) * np));
+    AMFLS_CUDA(cudaMalloc(&T.val, sizeof(double) * np));
+    for (Side* sd : {&A, &T}) {
+        AMFLS_CUDA(cudaMemsetAsync(sd->idx + nnz, 0, sizeof(int) * (np - nnz), stream));
+        AMFLS_CUDA(cudaMemsetAsync(sd->val + nnz, 0, sizeof(double) * (np - nnz), stream));
+        AMFLS_CUDA(cudaMalloc(&sd->off32, sizeof(int) * padded(sd->count + 1)));
+        AMFLS_CUDA(cudaMemsetAsync(sd->off32, 0, sizeof(int) * padded(sd->count + 1), stream));
+    }
     AMFLS_CUDA(cudaMemcpyAsync(A.off, d_off, sizeof(long long) * (rows_ + 1),
                                cudaMemcpyDeviceToDevice, stream));
     if (nnz > 0)
@@ -546,6 +588,19 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
     AMFLS_LAUNCHED();
     build_bins(T, bins, stream);
 
+    // int32 offsets and tilings of both sides for the streamed products
+    for (Side* sd : {&A, &T}) {
+        narrow_offsets_kernel<<<setup_grid(sd->count + 1), 256, 0, stream>>>(sd->off, sd->count,
+                                                                             sd->off32);
+        AMFLS_LAUNCHED();
+        std::vector<long long> host_off(sd->count + 1);
+        AMFLS_CUDA(cudaMemcpyAsync(host_off.data(), sd->off, sizeof(long long) * (sd->count + 1),
+                                   cudaMemcpyDeviceToHost, stream));
+        AMFLS_CUDA(cudaStreamSynchronize(stream));
+        make_tiles(host_off, sd->count, csr_tiles::kE1, 1, sd->one, stream);
+        make_tiles(host_off, sd->count, csr_tiles::kEC, 8, sd->many, stream);
+    }
+
     // certified norm model
     norm_model_kernel<<<setup_grid(rows_), 256, 0, stream>>>(A.off, A.val, rows_, 0, w->row_acc,
                                                             nullptr, nullptr, nullptr);
@@ -594,11 +649,9 @@ void CsrOperator::fill_ids(int* ids, long long n, cudaStream_t stream) {
 bool CsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
                            cudaStream_t stream) const {
     const Side& s = transpose ? *t_ : *a_;
-    const int grid = grid_for(s.bins.warp_start[6]);
-    spmv_binned_kernel<<<grid, kThreads, 0, stream>>>(
-        s.off, s.idx, s.val, s.perm, s.bins, x, ep,
-        ep.partials ? ep.partials : scratch_, ep.counter ? ep.counter : counter_);
-    AMFLS_LAUNCHED();
+    launch_tiles<1, true>(s.off32, s.idx, s.val, s.one, x, nullptr, 0, 1, ep,
+                          ep.partials ? ep.partials : scratch_, ep.counter ? ep.counter : counter_,
+                          stream);
     return true;
 }
 
@@ -609,18 +662,41 @@ void CsrOperator::product(bool transpose, const double* x, int block_cols, doubl
     const Side& s = transpose ? *t_ : *a_;
     const long long ldx = transpose ? rows_ : cols_;
     const long long ldy = transpose ? cols_ : rows_;
-    const int grid = grid_for(s.bins.warp_start[6]);
     if (block_cols == 1) {
         Epilogue ep;
         ep.out = y;
         product1(transpose, x, ep, stream);
         return;
     }
+    const Epilogue none;
+    const int tgrid = setup_grid(ldx);
     for (int c0 = 0; c0 < block_cols; c0 += 8) {
         const int nc = std::min(8, block_cols - c0);
-        spmm_binned_kernel<8><<<grid, kThreads, 0, stream>>>(
-            s.off, s.idx, s.val, s.perm, s.bins, x + c0 * ldx, ldx, y + c0 * ldy, ldy, nc);
-        AMFLS_LAUNCHED();
+        const double* xc = x + c0 * ldx;
+        double* yc = y + c0 * ldy;
+        if (nc > 4) {
+            rows_major_kernel<8><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows_);
+            AMFLS_LAUNCHED();
+            launch_tiles<8, false>(s.off32, s.idx, s.val, s.many, xrows_, yc, ldy, nc, none,
+                                   nullptr, nullptr, stream);
+        } else if (nc > 2) {
+            rows_major_kernel<4><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows_);
+            AMFLS_LAUNCHED();
+            launch_tiles<4, false>(s.off32, s.idx, s.val, s.many, xrows_, yc, ldy, nc, none,
+                                   nullptr, nullptr, stream);
+        } else if (nc == 2) {
+            rows_major_kernel<2><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows_);
+            AMFLS_LAUNCHED();
+            launch_tiles<2, false>(s.off32, s.idx, s.val, s.many, xrows_, yc, ldy, nc, none,
+                                   nullptr, nullptr, stream);
+        } else
+            launch_tiles<1, true>(s.off32, s.idx, s.val, s.one, xc, nullptr, 0, 1,
+                                  [&] {
+                                      Epilogue ep;
+                                      ep.out = yc;
+                                      return ep;
+                                  }(),
+                                  scratch_, counter_, stream);
     }
 }
 

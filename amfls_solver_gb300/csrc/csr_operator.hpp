@@ -62,6 +62,9 @@ private:
     std::unique_ptr<Side> t_;
     double* scratch_ = nullptr;
     unsigned* counter_ = nullptr;
+    // row-major staging of a multi-column input block (max(rows, cols) x 8);
+    // multi-column products on one operator are therefore stream-ordered
+    double* xrows_ = nullptr;
 };
 
 }  // namespace amfls_gpu

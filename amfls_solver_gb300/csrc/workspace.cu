@@ -499,12 +499,15 @@ __global__ void projected_solve_kernel(const double* alpha, const double* beta, 
             rhobar = r;
         }
         if (j + 1 < rows_t) {
+            // rotate rows (j, j+1): [phi_j; phibar_j+1] = G [phibar_j; g_j+1].
+            // g = U^T b is not a multiple of e_1 once U loses orthogonality,
+            // so g_j+1 enters both rotated entries.
             const double b = beta[j];
             const double r = hypot(rhobar, b);
             c = rhobar / r;
             s = b / r;
             rho[j] = r;
-            phi[j] = c * phibar;
+            phi[j] = c * phibar + s * g[j + 1];
             phibar = -s * phibar + c * g[j + 1];
         } else {
             rho[j] = rhobar;

@@ -105,6 +105,50 @@ def test_csr_products_match_reference(amfls, name):
     assert [sa, st] == list(data["steps"])
 
 
+def skewed_csr(seed=7, m=6000, n=6000):
+    """Rows of length 0..3 mixed with a few rows longer than one 2048-element
+    tile (split into slices) and a column present in every row (a transpose
+    row of m entries)."""
+    from amfls_solver_gb300 import problems
+
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 4, m)
+    lens[rng.choice(m, 6, replace=False)] = [300, 2047, 2048, 2049, 4500, n]
+    rows = []
+    for i, ln in enumerate(lens):
+        c = rng.choice(np.arange(1, n), min(int(ln), n - 1), replace=False)
+        rows.append(np.sort(np.concatenate([[0], c]) if i % 3 else c))
+    off = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int64)
+    col = np.concatenate(rows).astype(np.int64)
+    val = rng.standard_normal(col.size)
+    return problems.CsrProblem(m, n, off, col, val, np.zeros(m))
+
+
+def test_csr_tiled_products_long_and_empty_rows(amfls):
+    """Tiled products (row blocks, slices of long rows, empty rows) against
+    the oracle's sequential products within gamma_{2L+2} |A||x|, for 1..11
+    columns, and bit-identical on a repeat."""
+    prob = skewed_csr()
+    op = amfls.DeviceOperator(csr_tensor(prob))
+    ref = orc.Operator(prob)
+    rng = np.random.default_rng(3)
+    for s in (1, 2, 3, 5, 8, 11):
+        x = rng.standard_normal((prob.cols, s))
+        y = rng.standard_normal((prob.rows, s))
+        ax = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+        aty = op.apply(torch.from_numpy(y).cuda(), transpose=True).cpu().numpy()
+        ax_ref = ref.apply(np.asfortranarray(x))
+        aty_ref = ref.apply_transpose(np.asfortranarray(y))
+        for c in range(s):
+            assert np.all(np.abs(ax[:, c] - ax_ref[:, c]) <= 2 * product_bound(prob, x[:, c], False))
+            assert np.all(np.abs(aty[:, c] - aty_ref[:, c]) <=
+                          2 * product_bound(prob, y[:, c], True))
+        again = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+        assert np.array_equal(ax, again)
+    lens = np.diff(prob.row_offsets)
+    assert np.all(ax[lens == 0] == 0.0)
+
+
 @pytest.mark.parametrize("name", ["dense_model_rm", "dense_model_cm"])
 def test_dense_model_matches_reference(amfls, name):
     data, prob = load_golden(name)
