@@ -266,7 +266,8 @@ struct TileStore {
 };
 
 // Greedy cut of rows [0, count) with host offsets `off` into row blocks of at
-// most E nonzeros and E rows, and E-element slices of longer rows.
+// most E nonzeros and E rows, single rows of up to kRowTaskTiles E nonzeros,
+// and kRowTaskTiles E-element slices of longer rows (see csr_tiles.cuh).
 void make_tiles(const std::vector<long long>& off, int count, int E, int C, TileStore& ts,
                 cudaStream_t stream) {
     std::vector<int4> tiles;
@@ -275,13 +276,20 @@ void make_tiles(const std::vector<long long>& off, int count, int E, int C, Tile
     int r = 0;
     while (r < count) {
         const long long len = off[r + 1] - off[r];
-        if (len > E) {
+        const long long task = (long long)csr_tiles::kRowTaskTiles * E;
+        if (len > task) {  // slices of one warp task each
             const int first = (int)tiles.size();
-            for (long long e = off[r]; e < off[r + 1]; e += E) {
-                tiles.push_back(make_int4(r, r + 1, (int)e, (int)std::min(e + E, off[r + 1])));
+            for (long long e = off[r]; e < off[r + 1]; e += task) {
+                tiles.push_back(make_int4(r, r + 1, (int)e, (int)std::min(e + task, off[r + 1])));
                 split.push_back((int)long_rows.size());
             }
             long_rows.push_back(make_int2(first, (int)tiles.size() - first));
+            ++r;
+            continue;
+        }
+        if (len > E) {  // one warp task for the whole row
+            tiles.push_back(make_int4(r, r + 1, (int)off[r], (int)off[r + 1]));
+            split.push_back(-2);
             ++r;
             continue;
         }

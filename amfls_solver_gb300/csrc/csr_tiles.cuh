@@ -2,8 +2,9 @@
 //
 // A side of the operator (A or its stored transpose) is cut once, on the
 // host, into tiles: a tile is either a run of consecutive rows whose
-// nonzeros total at most E (and at most E rows), or, for a row longer than
-// E, one E-element slice of that row.  Every warp of the grid walks its own
+// nonzeros total at most E (and at most E rows), a single row of up to
+// kRowTaskTiles E nonzeros, or a kRowTaskTiles E-element slice of a longer
+// row.  Every warp of the grid walks its own
 // tiles (warp w takes tiles w, w + W, ... with W warps in the grid) and no
 // warp waits on another, so the only synchronisation is __syncwarp and an
 // SM keeps many independent tiles in flight.  Work on a tile:
@@ -18,12 +19,14 @@
 //      order of the reference's SparseCsrOperator::apply
 //      (src/algorithms/mathematics/operators/sparse_csr_operator.cpp:203-235),
 //      so those rows come out bit for bit equal to it; a longer row in the
-//      tile is summed by the whole warp (strided lanes, fixed butterfly);
+//      tile is summed by 8 lanes (strided, fixed butterfly), four at a time;
 //   3. results: each row's sum goes out through the fused epilogue (one
 //      column) or into the column-major output block.
-// A slice of a long row is summed by the warp; the slices' partial sums go
-// to global memory and the slice that arrives last (atomic ticket) adds them
-// in slice order.  Every sum is taken in an order fixed by the matrix, so
+// A long row (or slice) is streamed through registers by the warp -- E / 32
+// values, indices and gathers per lane in flight per step, lanes strided by
+// element, then a fixed butterfly -- without shared memory.  Slices' partial
+// sums go to global memory and the slice that arrives last (atomic ticket)
+// adds them in slice order.  Every sum is taken in an order fixed by the matrix, so
 // results are deterministic.  For C > 1 columns x is staged row-major
 // beforehand so that one gather reads C contiguous doubles.
 #pragma once
@@ -43,22 +46,30 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kE1 = 256;     // elements per tile, single-column products
 constexpr int kEC = 64;      // elements per tile, 2..8 columns
 constexpr int kSeqMax = 64;  // longest row summed by a single lane
+constexpr int kRowTaskTiles = 16;  // a row of up to 16 E nonzeros is one warp task
 static_assert(kEC <= kSeqMax, "multi-column tiles sum every row sequentially");
 
 struct Table {
     const int4* tiles = nullptr;      // {first row, end row, first element, end element}
-    const int* split = nullptr;       // long-row id of a slice tile, -1 for a row block
+    // -1: a row block; -2: one whole row of more than E nonzeros; q >= 0: a
+    // slice of long row q (rows longer than kRowTaskTiles E)
+    const int* split = nullptr;
     const int2* long_rows = nullptr;  // {first slice tile, slice count}
     unsigned* long_count = nullptr;   // arrival tickets, zero between launches
     double* long_part = nullptr;      // C partial sums per tile
     int ntiles = 0;
 };
 
-// Shared memory of one warp: values and gathered x (E x C), row offsets.
+// Shared memory of one warp: values and gathered x (E x C), row offsets
+// (E + 1) and the list of rows longer than kSeqMax (fewer than E / kSeqMax).
+// Rounded up to 16 bytes so that every warp's buffers stay aligned for the
+// 16-byte accesses to x.
 template <int C, int E>
 constexpr int warp_smem_bytes() {
-    return E * 8 + E * C * 8 + (E + 8) * 4;
+    return (E * 8 + E * C * 8 + (E + 8 + E / kSeqMax) * 4 + 15) / 16 * 16;
 }
+static_assert(warp_smem_bytes<8, kEC>() % 16 == 0 && warp_smem_bytes<1, kE1>() % 16 == 0,
+              "per-warp buffers must keep 16-byte alignment");
 
 template <int C, int E>
 constexpr int smem_bytes() {
@@ -88,6 +99,72 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
         const int R = d.y - d.x, n = d.w - d.z;
         const int q = tb.split[t];
 
+        if (q != -1) {
+            // a whole long row (q == -2) or a slice of one (q >= 0), through
+            // registers: group g = lane / C takes elements g, g + 32 / C, ...,
+            // lane c of the group column c
+            constexpr int kG = 32 / C;
+            const int g = lane / C, cl = lane % C;
+            double part = 0.0;
+            for (int base = d.z; base < d.w; base += E) {
+                constexpr int kStep = E / kG;
+                double av[kStep], xv[kStep];
+                int jv[kStep];
+#pragma unroll
+                for (int u = 0; u < kStep; ++u) {
+                    const int e = base + g + kG * u;
+                    jv[u] = e < d.w ? __ldcs(idx + e) : -1;
+                    av[u] = e < d.w ? __ldcs(val + e) : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < kStep; ++u)
+                    xv[u] = jv[u] >= 0 ? __ldg(x + (long long)jv[u] * C + cl) : 0.0;
+#pragma unroll
+                for (int u = 0; u < kStep; ++u) part = fma(av[u], xv[u], part);
+            }
+            for (int o = 16; o >= C; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            double acc[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) acc[c] = __shfl_sync(0xffffffffu, part, c);
+            if (lane == 0) {
+                if (q == -2) {
+                    if constexpr (kFused) {
+                        epilogue_row(ep, d.x, acc[0], sq_t, sq_out, dot, mx_t, mx_out, nonfin);
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < C; ++c)
+                            if (c < ncols) y[d.x + c * ldy] = acc[c];
+                    }
+                } else {
+                    const int2 lr = tb.long_rows[q];
+#pragma unroll
+                    for (int c = 0; c < C; ++c) tb.long_part[(long long)t * C + c] = acc[c];
+                    __threadfence();
+                    const unsigned ticket = atomicAdd(&tb.long_count[q], 1u);
+                    if (ticket == static_cast<unsigned>(lr.y - 1)) {
+                        tb.long_count[q] = 0u;
+                        __threadfence();
+                        double sum[C];
+#pragma unroll
+                        for (int c = 0; c < C; ++c) sum[c] = 0.0;
+                        for (int u = 0; u < lr.y; ++u)
+#pragma unroll
+                            for (int c = 0; c < C; ++c)
+                                sum[c] += __ldcg(&tb.long_part[(long long)(lr.x + u) * C + c]);
+                        if constexpr (kFused) {
+                            epilogue_row(ep, d.x, sum[0], sq_t, sq_out, dot, mx_t, mx_out,
+                                         nonfin);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < C; ++c)
+                                if (c < ncols) y[d.x + c * ldy] = sum[c];
+                        }
+                    }
+                }
+            }
+            continue;
+        }
+
         // 1. loads and gathers
         double a[kPer];
         int j[kPer];
@@ -97,8 +174,7 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
             j[u] = i < n ? __ldcs(idx + d.z + i) : -1;
             a[u] = i < n ? __ldcs(val + d.z + i) : 0.0;
         }
-        if (q < 0)
-            for (int i = lane; i <= R; i += 32) ro[i] = __ldcs(off + d.x + i) - d.z;
+        for (int i = lane; i <= R; i += 32) ro[i] = __ldcs(off + d.x + i) - d.z;
         if constexpr (C == 1) {
             double xv[kPer];
 #pragma unroll
@@ -125,7 +201,7 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
         __syncwarp();
 
         // 2./3. row sums and results
-        if (q < 0 && C > 1) {
+        if constexpr (C > 1) {
             // C lanes per row (lane c of the group takes column c), 32 / C rows
             // at a time; rows of these tiles have at most kEC <= kSeqMax nonzeros
             constexpr int kGroups = 32 / C;
@@ -136,7 +212,7 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                 for (int e = b0; e < b1; ++e) acc = fma(vs[e], xs[e * C + c], acc);
                 if (c < ncols) y[d.x + i + c * ldy] = acc;
             }
-        } else if (q < 0) {
+        } else {
             unsigned wide = 0;  // bit k: row lane + 32 k is left to the whole warp
             for (int k = 0, i = lane; i < R; ++k, i += 32) {
                 const int b0 = ro[i], b1 = ro[i + 1];
@@ -175,80 +251,32 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                         if (c < ncols) y[r + c * ldy] = acc[c];
                 }
             }
-            // rows longer than kSeqMax: the whole warp, one row at a time
+            // rows longer than kSeqMax (fewer than E / kSeqMax of them): listed
+            // after the row offsets, then summed four at a time by 8-lane
+            // groups (strided lanes, fixed butterfly within the group)
+            int* wl = ro + E + 1;
+            int nw = 0;
             for (int k = 0; k * 32 < R; ++k) {
-                unsigned pending = __ballot_sync(0xffffffffu, (wide >> k) & 1u);
-                while (pending) {
-                    const int src = __ffs(pending) - 1;
-                    pending &= pending - 1;
-                    const int i = src + 32 * k;
-                    const int b0 = ro[i], b1 = ro[i + 1];
-                    double acc[C];
-#pragma unroll
-                    for (int c = 0; c < C; ++c) acc[c] = 0.0;
-                    for (int e = b0 + lane; e < b1; e += 32) {
-                        const double av = vs[e];
-#pragma unroll
-                        for (int c = 0; c < C; ++c) acc[c] = fma(av, xs[e * C + c], acc[c]);
-                    }
-#pragma unroll
-                    for (int c = 0; c < C; ++c)
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1)
-                            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-                    if (lane == 0) {
-                        const int r = d.x + i;
-                        if constexpr (kFused) {
-                            epilogue_row(ep, r, acc[0], sq_t, sq_out, dot, mx_t, mx_out, nonfin);
-                        } else {
-#pragma unroll
-                            for (int c = 0; c < C; ++c)
-                                if (c < ncols) y[r + c * ldy] = acc[c];
-                        }
-                    }
-                }
+                const unsigned bits = __ballot_sync(0xffffffffu, (wide >> k) & 1u);
+                if ((wide >> k) & 1u) wl[nw + __popc(bits & ((1u << lane) - 1u))] = lane + 32 * k;
+                nw += __popc(bits);
             }
-        } else {
-            // a slice of one long row: lane groups of C (lane c, column c)
-            // stride over the elements, then a fixed butterfly over the groups
-            double acc[C];
+            __syncwarp();
+            const int g = lane >> 3, gl = lane & 7;
+            for (int w0 = 0; w0 < nw; w0 += 4) {
+                const bool mine = w0 + g < nw;
+                const int i = mine ? wl[w0 + g] : 0;
+                const int b0 = mine ? ro[i] : 0, b1 = mine ? ro[i + 1] : 0;
+                double acc = 0.0;
+                for (int e = b0 + gl; e < b1; e += 8) acc = fma(vs[e], xs[e], acc);
 #pragma unroll
-            for (int c = 0; c < C; ++c) acc[c] = 0.0;
-            if constexpr (C == 1) {
-                for (int e = lane; e < n; e += 32) acc[0] = fma(vs[e], xs[e], acc[0]);
-                for (int o = 16; o > 0; o >>= 1)
-                    acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
-            } else {
-                const int g = lane / C, cl = lane % C;
-                double part = 0.0;
-                for (int e = g; e < n; e += 32 / C) part = fma(vs[e], xs[e * C + cl], part);
-                for (int o = 16; o >= C; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                // lane c (group 0) now holds column c; hand every column to lane 0
-#pragma unroll
-                for (int c = 0; c < C; ++c) acc[c] = __shfl_sync(0xffffffffu, part, c);
-            }
-            if (lane == 0) {
-                const int2 lr = tb.long_rows[q];
-#pragma unroll
-                for (int c = 0; c < C; ++c) tb.long_part[(long long)t * C + c] = acc[c];
-                __threadfence();
-                const unsigned ticket = atomicAdd(&tb.long_count[q], 1u);
-                if (ticket == static_cast<unsigned>(lr.y - 1)) {
-                    tb.long_count[q] = 0u;
-                    __threadfence();
-                    double sum[C];
-#pragma unroll
-                    for (int c = 0; c < C; ++c) sum[c] = 0.0;
-                    for (int u = 0; u < lr.y; ++u)
-#pragma unroll
-                        for (int c = 0; c < C; ++c)
-                            sum[c] += __ldcg(&tb.long_part[(long long)(lr.x + u) * C + c]);
+                for (int o = 4; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (mine && gl == 0) {
+                    const int r = d.x + i;
                     if constexpr (kFused) {
-                        epilogue_row(ep, d.x, sum[0], sq_t, sq_out, dot, mx_t, mx_out, nonfin);
+                        epilogue_row(ep, r, acc, sq_t, sq_out, dot, mx_t, mx_out, nonfin);
                     } else {
-#pragma unroll
-                        for (int c = 0; c < C; ++c)
-                            if (c < ncols) y[d.x + c * ldy] = sum[c];
+                        y[r] = acc;
                     }
                 }
             }
