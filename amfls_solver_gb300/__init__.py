@@ -2,7 +2,9 @@
 
 Drop-in for the reference's python/amfls package on CUDA tensors:
 ``run_amfls``, ``run_fixed_rbgk``, ``SolveResult``, ``load_library`` and
-``torch.ops.amfls.run_amfls`` / ``run_fixed_rbgk`` with the reference's schema.
+``torch.ops.amfls.run_amfls`` / ``run_fixed_rbgk`` with the reference's schema,
+plus the mixed-precision form ``run_amfls_mixed`` (FP32 / BF16 inner solves
+refined in FP64).
 The compute path is the native library libamfls_gb300.so (C ABI in
 include/amfls_gpu.h); importing this package never falls back to the CPU.
 """
@@ -12,6 +14,7 @@ from .binding import (
     load_library,
     register_torch_ops,
     run_amfls,
+    run_amfls_mixed,
     run_fixed_rbgk,
 )
 
@@ -21,5 +24,6 @@ __all__ = [
     "load_library",
     "register_torch_ops",
     "run_amfls",
+    "run_amfls_mixed",
     "run_fixed_rbgk",
 ]

@@ -51,6 +51,7 @@ EXPORTED = [
     "amfls_gpu_operator_relative_block_product_cost",
     "amfls_gpu_operator_validation_error_model", "amfls_gpu_solve_amfls",
     "amfls_gpu_solve_fixed_rbgk", "amfls_gpu_dense_apply_transpose_noalloc",
+    "amfls_gpu_reduced_operator_create", "amfls_gpu_solve_amfls_mixed",
 ]
 
 
@@ -92,6 +93,9 @@ def load():
     for name in ("amfls_gpu_solve_amfls", "amfls_gpu_solve_fixed_rbgk"):
         getattr(lib, name).argtypes = [P, P, ctypes.POINTER(Options), P, ctypes.POINTER(Result),
                                        P, P, I, P]
+    lib.amfls_gpu_reduced_operator_create.argtypes = [P, I, P, ctypes.POINTER(P)]
+    lib.amfls_gpu_solve_amfls_mixed.argtypes = [P, P, P, ctypes.POINTER(Options), D, I, P,
+                                                ctypes.POINTER(Result), P, P, I, P]
     _lib = lib
     return lib
 

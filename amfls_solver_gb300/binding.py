@@ -241,6 +241,23 @@ class DeviceOperator:
         return _native.load().amfls_gpu_operator_relative_block_product_cost(
             self.handle, block_cols)
 
+    def reduced(self, values: str = "fp32") -> "DeviceOperator":
+        """The same matrix with values rounded to FP32 or BF16 (products in
+        FP32); part of the mixed-precision form.  Keeps this operator alive."""
+        codes = {"fp32": 1, "bf16": 2}
+        if values not in codes:
+            raise ValueError("values must be 'fp32' or 'bf16'")
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _native.check(_native.load().amfls_gpu_reduced_operator_create(
+                self.handle, codes[values], _stream_handle(self.device), ctypes.byref(handle)))
+        op = DeviceOperator.__new__(DeviceOperator)
+        op.rows, op.cols, op.device = self.rows, self.cols, self.device
+        op.handle = handle
+        op._keep = self  # a reduced CSR operator shares the source's index arrays
+        op.values = values
+        return op
+
 
 # --------------------------------------------------------------- solves ----
 
@@ -270,6 +287,50 @@ def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options: _na
 
 def _uint64(v: int) -> int:
     return int(v) & (2**64 - 1)
+
+
+def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
+                    inner_tolerance: float = 1e-6, maximum_refinements: int = 8,
+                    regularization: float = 0.0, tolerance: float = 1e-8,
+                    failure_probability: float = 1e-6, maximum_epochs: int = 0,
+                    maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
+                    maximum_basis_size: int = 0, seed: int = 0, stream: int = 0,
+                    reduced: "DeviceOperator | None" = None) -> SolveResult:
+    """Mixed-precision AMFLS: FP32 (or BF16-stored) inner solves refined in
+    FP64; the certified FP64 validation on the original matrix decides
+    termination.  `matrix` is a CUDA tensor or a DeviceOperator; `reduced`
+    reuses an existing reduced operator.  Work limits apply to each inner
+    solve.  No counterpart in the reference."""
+    op = matrix if isinstance(matrix, DeviceOperator) else DeviceOperator(matrix)
+    if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
+        raise ValueError("b must be a float64 CUDA vector of length rows on the matrix's device")
+    low = reduced if reduced is not None else op.reduced(values)
+    o = _native.default_options()
+    o.regularization = float(regularization)
+    o.tolerance = float(tolerance)
+    o.failure_probability = float(failure_probability)
+    o.maximum_epochs = int(maximum_epochs)
+    o.maximum_depth = int(maximum_depth)
+    o.maximum_auxiliary_width = int(maximum_auxiliary_width)
+    o.maximum_basis_size = int(maximum_basis_size)
+    o.seed = _uint64(seed)
+    o.stream = _uint64(stream)
+    b = b.contiguous()
+    x = torch.empty(op.cols, dtype=torch.float64, device=b.device)
+    res = _native.Result()
+    tf = np.zeros((TRACE_CAPACITY, 29))
+    ti = np.zeros((TRACE_CAPACITY, 4), dtype=np.int64)
+    with torch.cuda.device(b.device):
+        _native.check(_native.load().amfls_gpu_solve_amfls_mixed(
+            op.handle, low.handle, b.data_ptr(), ctypes.byref(o), float(inner_tolerance),
+            int(maximum_refinements), x.data_ptr(), ctypes.byref(res), tf.ctypes.data,
+            ti.ctypes.data, TRACE_CAPACITY, _stream_handle(b.device)))
+    rows = min(res.trace_rows, TRACE_CAPACITY)
+    return _decode((x, torch.tensor(list(res.metrics), dtype=torch.float64),
+                    torch.tensor(list(res.counters), dtype=torch.int64),
+                    torch.tensor(list(res.timings), dtype=torch.float64),
+                    torch.from_numpy(tf[:rows].copy()), torch.from_numpy(ti[:rows].copy()),
+                    int(res.status), int(res.stop_reason)))
 
 
 def _run_amfls_impl(matrix, b, regularization, tolerance, failure_probability,

@@ -11,6 +11,7 @@
 #include "controller.hpp"
 #include "csr_operator.hpp"
 #include "dense_operator.hpp"
+#include "reduced_operator.hpp"
 
 struct amfls_gpu_operator {
     std::unique_ptr<amfls_gpu::DeviceOperator> impl;
@@ -218,6 +219,43 @@ int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
         if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
         const auto r = amfls_gpu::solve_fixed_rbgk(deref(op), d_b, to_options(options),
                                                    d_solution, as_stream(stream));
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+    });
+}
+
+int amfls_gpu_reduced_operator_create(const amfls_gpu_operator* source, int value_type,
+                                      void* stream, amfls_gpu_operator** out) {
+    return guarded([&] {
+        if (out == nullptr) throw std::invalid_argument("output handle must not be null");
+        *out = nullptr;
+        if (value_type != AMFLS_GPU_VALUES_FP32 && value_type != AMFLS_GPU_VALUES_BF16)
+            throw std::invalid_argument("value_type must be FP32 (1) or BF16 (2)");
+        const auto type = value_type == AMFLS_GPU_VALUES_FP32 ? amfls_gpu::ValueType::fp32
+                                                              : amfls_gpu::ValueType::bf16;
+        const amfls_gpu::DeviceOperator& src = deref(source);
+        auto h = std::make_unique<amfls_gpu_operator>();
+        if (const auto* csr = dynamic_cast<const amfls_gpu::CsrOperator*>(&src))
+            h->impl = std::make_unique<amfls_gpu::ReducedCsrOperator>(*csr, type, as_stream(stream));
+        else if (const auto* dense = dynamic_cast<const amfls_gpu::DenseOperator*>(&src))
+            h->impl =
+                std::make_unique<amfls_gpu::ReducedDenseOperator>(*dense, type, as_stream(stream));
+        else
+            throw std::invalid_argument("the source must be an FP64 CSR or dense operator");
+        *out = h.release();
+    });
+}
+
+int amfls_gpu_solve_amfls_mixed(const amfls_gpu_operator* op, const amfls_gpu_operator* reduced,
+                                const double* d_b, const amfls_gpu_options* options,
+                                double inner_tolerance, int maximum_refinements,
+                                double* d_solution, amfls_gpu_result* result,
+                                double* trace_float, int64_t* trace_int, int trace_capacity,
+                                void* stream) {
+    return guarded([&] {
+        const auto r = amfls_gpu::solve_amfls_mixed(deref(op), deref(reduced), d_b,
+                                                    to_options(options), inner_tolerance,
+                                                    maximum_refinements, d_solution,
+                                                    as_stream(stream));
         export_result(r, result, trace_float, trace_int, trace_capacity);
     });
 }

@@ -73,6 +73,24 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
 SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b,
                              const SolveOptions& options, double* d_solution, cudaStream_t stream);
 
+// One outer step of the mixed-precision solve: the inner solve's outcome and
+// the FP64 certificate of the refined x.
+struct RefinementStep {
+    int inner_status, inner_stop_reason, inner_depth, inner_basis_rank;
+    double certificate;
+};
+
+// Mixed-precision form (mixed.cu): inner AMFLS solves on `reduced` (an FP32
+// or BF16 copy of `op`, or any operator of its shape) to `inner_tolerance`,
+// refined in FP64 until op's certified validation meets options.tolerance.
+// The result's validation fields, status and stop reason are those of the
+// last FP64 validation; depth and iterations add up the inner solves.
+SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& reduced,
+                              const double* d_b, const SolveOptions& options,
+                              double inner_tolerance, int maximum_refinements,
+                              double* d_solution, cudaStream_t stream,
+                              std::vector<RefinementStep>* steps = nullptr);
+
 // Result tensors in the torch binding's layout (bindings/torch/result_tensors.hpp:12-156).
 void pack_metrics(const SolveResult& r, double out[21]);
 void pack_counters(const SolveResult& r, long long out[36]);

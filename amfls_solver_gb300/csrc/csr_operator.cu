@@ -20,12 +20,14 @@
 // sequentially in the reference's order (rows in CSR order, columns in row
 // order), so those stored sums match the reference bit for bit.
 #include <cub/cub.cuh>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <memory>
 #include <stdexcept>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -338,31 +340,31 @@ __global__ void rows_major_kernel(const double* __restrict__ x, long long ld, in
 
 // Resident CTAs for a tile kernel (every warp of the grid walks its own
 // tiles), at most one warp per tile and at most kMaxBlocks CTAs.
-template <int C, int E, bool kFused>
+template <typename V, int C, int E, bool kFused>
 int tile_grid(int ntiles) {
     static int per_sm = -1, sms = 0;
     if (per_sm < 0) {
         constexpr int bytes = csr_tiles::smem_bytes<C, E>();
-        AMFLS_CUDA(cudaFuncSetAttribute(csr_tiles::tile_product_kernel<C, E, kFused>,
+        AMFLS_CUDA(cudaFuncSetAttribute(csr_tiles::tile_product_kernel<V, C, E, kFused>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         int dev = 0, nb = 0;
         AMFLS_CUDA(cudaGetDevice(&dev));
         AMFLS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, csr_tiles::tile_product_kernel<C, E, kFused>, csr_tiles::kThreads, bytes));
+            &nb, csr_tiles::tile_product_kernel<V, C, E, kFused>, csr_tiles::kThreads, bytes));
         per_sm = std::max(1, nb);
     }
     const int need = (ntiles + csr_tiles::kWarps - 1) / csr_tiles::kWarps;
     return std::max(1, std::min({need, per_sm * sms, kMaxBlocks}));
 }
 
-template <int C, bool kFused>
-void launch_tiles(const int* off, const int* idx, const double* val, const TileStore& ts,
+template <int C, bool kFused, typename V>
+void launch_tiles(const int* off, const int* idx, const V* val, const TileStore& ts,
                   const double* x, double* y, long long ldy, int ncols, const Epilogue& ep,
                   double* partials, unsigned* counter, cudaStream_t stream) {
     constexpr int E = C == 1 ? csr_tiles::kE1 : csr_tiles::kEC;
-    const int grid = tile_grid<C, E, kFused>(ts.ntiles);
-    csr_tiles::tile_product_kernel<C, E, kFused>
+    const int grid = tile_grid<V, C, E, kFused>(ts.ntiles);
+    csr_tiles::tile_product_kernel<V, C, E, kFused>
         <<<grid, csr_tiles::kThreads, csr_tiles::smem_bytes<C, E>(), stream>>>(
             off, idx, val, ts.view(), x, y, ldy, ncols, ep, partials, counter);
     AMFLS_LAUNCHED();
@@ -654,12 +656,70 @@ void CsrOperator::fill_ids(int* ids, long long n, cudaStream_t stream) {
     AMFLS_LAUNCHED();
 }
 
+namespace {
+
+// Single-column product of one side with a fused epilogue.
+template <typename V>
+void side_product1(const int* off32, const int* idx, const V* vals, const TileStore& one,
+                   const double* x, const Epilogue& ep, double* partials, unsigned* counter,
+                   cudaStream_t stream) {
+    launch_tiles<1, true>(off32, idx, vals, one, x, nullptr, 0, 1, ep, partials, counter, stream);
+}
+
+// Block product of one side: eight columns per pass, each pass staging its
+// columns row-major in `xrows` (ldx x 8).
+template <typename V>
+void side_block(const int* off32, const int* idx, const V* vals, const TileStore& one,
+                const TileStore& many, const double* x, long long ldx, int block_cols,
+                double* y, long long ldy, double* xrows, double* partials, unsigned* counter,
+                cudaStream_t stream) {
+    const Epilogue none;
+    const int tgrid = setup_grid(ldx);
+    for (int c0 = 0; c0 < block_cols; c0 += 8) {
+        const int nc = std::min(8, block_cols - c0);
+        const double* xc = x + c0 * ldx;
+        double* yc = y + c0 * ldy;
+        if (nc > 4) {
+            rows_major_kernel<8><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows);
+            AMFLS_LAUNCHED();
+            launch_tiles<8, false>(off32, idx, vals, many, xrows, yc, ldy, nc, none, nullptr,
+                                   nullptr, stream);
+        } else if (nc > 2) {
+            rows_major_kernel<4><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows);
+            AMFLS_LAUNCHED();
+            launch_tiles<4, false>(off32, idx, vals, many, xrows, yc, ldy, nc, none, nullptr,
+                                   nullptr, stream);
+        } else if (nc == 2) {
+            rows_major_kernel<2><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows);
+            AMFLS_LAUNCHED();
+            launch_tiles<2, false>(off32, idx, vals, many, xrows, yc, ldy, nc, none, nullptr,
+                                   nullptr, stream);
+        } else {
+            Epilogue ep;
+            ep.out = yc;
+            side_product1(off32, idx, vals, one, xc, ep, partials, counter, stream);
+        }
+    }
+}
+
+template <typename V>
+__global__ void narrow_values_kernel(const double* in, long long n, V* out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        if constexpr (std::is_same_v<V, float>)
+            out[i] = __double2float_rn(in[i]);
+        else
+            out[i] = __double2bfloat16(in[i]);
+    }
+}
+
+}  // namespace
+
 bool CsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
                            cudaStream_t stream) const {
     const Side& s = transpose ? *t_ : *a_;
-    launch_tiles<1, true>(s.off32, s.idx, s.val, s.one, x, nullptr, 0, 1, ep,
-                          ep.partials ? ep.partials : scratch_, ep.counter ? ep.counter : counter_,
-                          stream);
+    side_product1(s.off32, s.idx, s.val, s.one, x, ep, ep.partials ? ep.partials : scratch_,
+                  ep.counter ? ep.counter : counter_, stream);
     return true;
 }
 
@@ -668,44 +728,98 @@ void CsrOperator::product(bool transpose, const double* x, int block_cols, doubl
     if (x == nullptr || y == nullptr || block_cols <= 0)
         throw std::invalid_argument("CSR product block is invalid");
     const Side& s = transpose ? *t_ : *a_;
-    const long long ldx = transpose ? rows_ : cols_;
-    const long long ldy = transpose ? cols_ : rows_;
-    if (block_cols == 1) {
-        Epilogue ep;
-        ep.out = y;
-        product1(transpose, x, ep, stream);
-        return;
+    side_block(s.off32, s.idx, s.val, s.one, s.many, x, transpose ? rows_ : cols_, block_cols, y,
+               transpose ? cols_ : rows_, xrows_, scratch_, counter_, stream);
+}
+
+// ------------------------------------------------- reduced precision ----
+
+ReducedCsrOperator::ReducedCsrOperator(const CsrOperator& src, ValueType type,
+                                       cudaStream_t stream)
+    : src_(src), type_(type) {
+    if (type != ValueType::fp32 && type != ValueType::bf16)
+        throw std::invalid_argument("reduced CSR values must be FP32 or BF16");
+    const long long np = padded(src.nnz_);
+    const size_t vb = type == ValueType::fp32 ? 4 : 2;
+    try {
+        for (int side = 0; side < 2; ++side) {
+            const double* in = side ? src.t_->val : src.a_->val;
+            AMFLS_CUDA(cudaMalloc(&vals_[side], vb * np));
+            AMFLS_CUDA(cudaMemsetAsync(vals_[side], 0, vb * np, stream));
+            if (src.nnz_ > 0) {
+                if (type == ValueType::fp32)
+                    narrow_values_kernel<float><<<setup_grid(src.nnz_), 256, 0, stream>>>(
+                        in, src.nnz_, static_cast<float*>(vals_[side]));
+                else
+                    narrow_values_kernel<__nv_bfloat16><<<setup_grid(src.nnz_), 256, 0, stream>>>(
+                        in, src.nnz_, static_cast<__nv_bfloat16*>(vals_[side]));
+                AMFLS_LAUNCHED();
+            }
+        }
+        AMFLS_CUDA(cudaMalloc(&xrows_, sizeof(double) * 8 * (size_t)std::max(src.rows_, src.cols_)));
+        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxBlocks + 64));
+        counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
+                                               sizeof(double) * 6 * kMaxBlocks);
+        AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
+        AMFLS_CUDA(cudaStreamSynchronize(stream));
+    } catch (...) {
+        release();
+        throw;
     }
-    const Epilogue none;
-    const int tgrid = setup_grid(ldx);
-    for (int c0 = 0; c0 < block_cols; c0 += 8) {
-        const int nc = std::min(8, block_cols - c0);
-        const double* xc = x + c0 * ldx;
-        double* yc = y + c0 * ldy;
-        if (nc > 4) {
-            rows_major_kernel<8><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows_);
-            AMFLS_LAUNCHED();
-            launch_tiles<8, false>(s.off32, s.idx, s.val, s.many, xrows_, yc, ldy, nc, none,
-                                   nullptr, nullptr, stream);
-        } else if (nc > 2) {
-            rows_major_kernel<4><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows_);
-            AMFLS_LAUNCHED();
-            launch_tiles<4, false>(s.off32, s.idx, s.val, s.many, xrows_, yc, ldy, nc, none,
-                                   nullptr, nullptr, stream);
-        } else if (nc == 2) {
-            rows_major_kernel<2><<<tgrid, 256, 0, stream>>>(xc, ldx, (int)ldx, nc, xrows_);
-            AMFLS_LAUNCHED();
-            launch_tiles<2, false>(s.off32, s.idx, s.val, s.many, xrows_, yc, ldy, nc, none,
-                                   nullptr, nullptr, stream);
-        } else
-            launch_tiles<1, true>(s.off32, s.idx, s.val, s.one, xc, nullptr, 0, 1,
-                                  [&] {
-                                      Epilogue ep;
-                                      ep.out = yc;
-                                      return ep;
-                                  }(),
-                                  scratch_, counter_, stream);
+    model_ = reduced_model(src.validation_error_model(), type);
+}
+
+ReducedCsrOperator::~ReducedCsrOperator() { release(); }
+
+void ReducedCsrOperator::release() {
+    for (void*& v : vals_) {
+        cudaFree(v);
+        v = nullptr;
     }
+    cudaFree(xrows_);
+    cudaFree(scratch_);
+    xrows_ = nullptr;
+    scratch_ = nullptr;
+}
+
+bool ReducedCsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
+                                  cudaStream_t stream) const {
+    const CsrOperator::Side& s = transpose ? *src_.t_ : *src_.a_;
+    double* partials = ep.partials ? ep.partials : scratch_;
+    unsigned* counter = ep.counter ? ep.counter : counter_;
+    const void* v = vals_[transpose ? 1 : 0];
+    if (type_ == ValueType::fp32)
+        side_product1(s.off32, s.idx, static_cast<const float*>(v), s.one, x, ep, partials,
+                      counter, stream);
+    else
+        side_product1(s.off32, s.idx, static_cast<const __nv_bfloat16*>(v), s.one, x, ep,
+                      partials, counter, stream);
+    return true;
+}
+
+void ReducedCsrOperator::product(bool transpose, const double* x, int block_cols, double* y,
+                                 cudaStream_t stream) const {
+    if (x == nullptr || y == nullptr || block_cols <= 0)
+        throw std::invalid_argument("CSR product block is invalid");
+    const CsrOperator::Side& s = transpose ? *src_.t_ : *src_.a_;
+    const long long ldx = transpose ? src_.rows_ : src_.cols_;
+    const long long ldy = transpose ? src_.cols_ : src_.rows_;
+    const void* v = vals_[transpose ? 1 : 0];
+    if (type_ == ValueType::fp32)
+        side_block(s.off32, s.idx, static_cast<const float*>(v), s.one, s.many, x, ldx,
+                   block_cols, y, ldy, xrows_, scratch_, counter_, stream);
+    else
+        side_block(s.off32, s.idx, static_cast<const __nv_bfloat16*>(v), s.one, s.many, x, ldx,
+                   block_cols, y, ldy, xrows_, scratch_, counter_, stream);
+}
+
+void ReducedCsrOperator::apply(const double* x, int block_cols, double* y, cudaStream_t s) const {
+    product(false, x, block_cols, y, s);
+}
+
+void ReducedCsrOperator::apply_transpose(const double* y, int block_cols, double* x,
+                                         cudaStream_t s) const {
+    product(true, y, block_cols, x, s);
 }
 
 void CsrOperator::apply(const double* x, int block_cols, double* y, cudaStream_t s) const {

@@ -7,6 +7,8 @@
 
 namespace amfls_gpu {
 
+class ReducedCsrOperator;
+
 class CsrOperator final : public DeviceOperator {
 public:
     // The CSR arrays are device pointers in the reference's layout: int64 row
@@ -40,6 +42,7 @@ public:
                   cudaStream_t s) const override;
 
 private:
+    friend class ReducedCsrOperator;
     struct Side;
     void build(const long long* d_off, const long long* d_idx, const double* d_val,
                cudaStream_t stream);
@@ -65,6 +68,44 @@ private:
     // row-major staging of a multi-column input block (max(rows, cols) x 8);
     // multi-column products on one operator are therefore stream-ordered
     double* xrows_ = nullptr;
+};
+
+// The matrix of a CsrOperator with its values rounded to FP32 or BF16 (one
+// rounding per entry, round to nearest): products read the stored values,
+// round x to FP32 and accumulate in FP32.  It shares the source operator's
+// structure, so the source must outlive it.  Its validation model is the
+// source's widened for the rounded values and FP32 accumulation (see
+// reduced_model), so certificates computed with it describe the rounded
+// matrix.  Part of the mixed-precision form; no counterpart in the reference.
+class ReducedCsrOperator final : public DeviceOperator {
+public:
+    ReducedCsrOperator(const CsrOperator& src, ValueType type, cudaStream_t stream);
+    ~ReducedCsrOperator() override;
+    ReducedCsrOperator(const ReducedCsrOperator&) = delete;
+    ReducedCsrOperator& operator=(const ReducedCsrOperator&) = delete;
+
+    int rows() const override { return src_.rows(); }
+    int cols() const override { return src_.cols(); }
+    int kind() const override { return 0; }
+    ValueType value_type() const { return type_; }
+    void apply(const double* x, int block_cols, double* y, cudaStream_t s) const override;
+    void apply_transpose(const double* y, int block_cols, double* x,
+                         cudaStream_t s) const override;
+    ValidationModel validation_error_model() const override { return model_; }
+    bool product1(bool transpose, const double* x, const Epilogue& ep,
+                  cudaStream_t s) const override;
+
+private:
+    void product(bool transpose, const double* x, int block_cols, double* y,
+                 cudaStream_t s) const;
+    void release();
+    const CsrOperator& src_;
+    ValueType type_;
+    void* vals_[2] = {nullptr, nullptr};  // A side, transpose side
+    double* xrows_ = nullptr;
+    double* scratch_ = nullptr;
+    unsigned* counter_ = nullptr;
+    ValidationModel model_;
 };
 
 }  // namespace amfls_gpu

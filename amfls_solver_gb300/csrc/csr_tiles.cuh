@@ -31,9 +31,11 @@
 // beforehand so that one gather reads C contiguous doubles.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 #include "epilogue.cuh"
@@ -60,6 +62,21 @@ struct Table {
     int ntiles = 0;
 };
 
+// Values stored as V; FP64 values accumulate in FP64 (the exact path), FP32
+// and BF16 values accumulate in FP32 with x rounded to FP32 on load.
+template <typename V>
+using acc_t = std::conditional_t<std::is_same_v<V, double>, double, float>;
+
+template <typename A>
+__device__ __forceinline__ A to_acc(double v) {
+    return static_cast<A>(v);
+}
+__device__ __forceinline__ float load_value(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ double load_value(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float load_value(const __nv_bfloat16* p) {
+    return __bfloat162float(*p);
+}
+
 // Shared memory of one warp: values and gathered x (E x C), row offsets
 // (E + 1) and the list of rows longer than kSeqMax (fewer than E / kSeqMax).
 // Rounded up to 16 bytes so that every warp's buffers stay aligned for the
@@ -76,19 +93,20 @@ constexpr int smem_bytes() {
     return kWarps * warp_smem_bytes<C, E>();
 }
 
-template <int C, int E, bool kFused>
+template <typename V, int C, int E, bool kFused>
 __global__ void __launch_bounds__(kThreads)
 tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
-                    const double* __restrict__ val, Table tb, const double* __restrict__ x,
+                    const V* __restrict__ val, Table tb, const double* __restrict__ x,
                     double* __restrict__ y, long long ldy, int ncols, Epilogue ep,
                     double* partials, unsigned* counter) {
     if (kFused && ep.guard && *ep.guard == 0) return;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char* wbase = smem + warp * warp_smem_bytes<C, E>();
-    double* vs = reinterpret_cast<double*>(wbase);  // E values
-    double* xs = vs + E;                            // E x C gathered x
-    int* ro = reinterpret_cast<int*>(xs + E * C);   // E + 1 row offsets
+    using A = acc_t<V>;
+    A* vs = reinterpret_cast<A*>(wbase);           // E values
+    A* xs = reinterpret_cast<A*>(wbase + E * 8);   // E x C gathered x
+    int* ro = reinterpret_cast<int*>(wbase + E * 8 + E * C * 8);  // E + 1 row offsets
     constexpr int kPer = E / 32;
 
     double sq_t = 0.0, sq_out = 0.0, dot = 0.0, mx_t = 0.0, mx_out = 0.0;
@@ -105,20 +123,20 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
             // lane c of the group column c
             constexpr int kG = 32 / C;
             const int g = lane / C, cl = lane % C;
-            double part = 0.0;
+            A part = 0;
             for (int base = d.z; base < d.w; base += E) {
                 constexpr int kStep = E / kG;
-                double av[kStep], xv[kStep];
+                A av[kStep], xv[kStep];
                 int jv[kStep];
 #pragma unroll
                 for (int u = 0; u < kStep; ++u) {
                     const int e = base + g + kG * u;
                     jv[u] = e < d.w ? __ldcs(idx + e) : -1;
-                    av[u] = e < d.w ? __ldcs(val + e) : 0.0;
+                    av[u] = e < d.w ? load_value(val + e) : A(0);
                 }
 #pragma unroll
                 for (int u = 0; u < kStep; ++u)
-                    xv[u] = jv[u] >= 0 ? __ldg(x + (long long)jv[u] * C + cl) : 0.0;
+                    xv[u] = jv[u] >= 0 ? to_acc<A>(__ldg(x + (long long)jv[u] * C + cl)) : A(0);
 #pragma unroll
                 for (int u = 0; u < kStep; ++u) part = fma(av[u], xv[u], part);
             }
@@ -166,19 +184,19 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
         }
 
         // 1. loads and gathers
-        double a[kPer];
+        A a[kPer];
         int j[kPer];
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
             const int i = lane + 32 * u;
             j[u] = i < n ? __ldcs(idx + d.z + i) : -1;
-            a[u] = i < n ? __ldcs(val + d.z + i) : 0.0;
+            a[u] = i < n ? load_value(val + d.z + i) : A(0);
         }
         for (int i = lane; i <= R; i += 32) ro[i] = __ldcs(off + d.x + i) - d.z;
         if constexpr (C == 1) {
-            double xv[kPer];
+            A xv[kPer];
 #pragma unroll
-            for (int u = 0; u < kPer; ++u) xv[u] = j[u] >= 0 ? __ldg(x + j[u]) : 0.0;
+            for (int u = 0; u < kPer; ++u) xv[u] = j[u] >= 0 ? to_acc<A>(__ldg(x + j[u])) : A(0);
 #pragma unroll
             for (int u = 0; u < kPer; ++u) {
                 vs[lane + 32 * u] = a[u];
@@ -192,9 +210,13 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                 if (j[u] >= 0) {
                     const double2* src =
                         reinterpret_cast<const double2*>(x + (long long)j[u] * C);
-                    double2* dst = reinterpret_cast<double2*>(xs + (lane + 32 * u) * C);
+                    A* dst = xs + (lane + 32 * u) * C;
 #pragma unroll
-                    for (int h = 0; h < C / 2; ++h) dst[h] = __ldg(src + h);
+                    for (int h = 0; h < C / 2; ++h) {
+                        const double2 p = __ldg(src + h);
+                        dst[2 * h] = to_acc<A>(p.x);
+                        dst[2 * h + 1] = to_acc<A>(p.y);
+                    }
                 }
             }
         }
@@ -208,9 +230,9 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
             const int g = lane / C, c = lane % C;
             for (int i = g; i < R; i += kGroups) {
                 const int b0 = ro[i], b1 = ro[i + 1];
-                double acc = 0.0;
+                A acc = 0;
                 for (int e = b0; e < b1; ++e) acc = fma(vs[e], xs[e * C + c], acc);
-                if (c < ncols) y[d.x + i + c * ldy] = acc;
+                if (c < ncols) y[d.x + i + c * ldy] = static_cast<double>(acc);
             }
         } else {
             unsigned wide = 0;  // bit k: row lane + 32 k is left to the whole warp
@@ -220,12 +242,12 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                     wide |= 1u << k;
                     continue;
                 }
-                double acc[C];
+                A acc[C];
 #pragma unroll
-                for (int c = 0; c < C; ++c) acc[c] = 0.0;
+                for (int c = 0; c < C; ++c) acc[c] = 0;
                 int e = b0;
                 for (; e + 4 <= b1; e += 4) {
-                    double av[4], xv[4][C];
+                    A av[4], xv[4][C];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         av[u] = vs[e + u];
@@ -238,17 +260,18 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                         for (int c = 0; c < C; ++c) acc[c] = fma(av[u], xv[u][c], acc[c]);
                 }
                 for (; e < b1; ++e) {
-                    const double av = vs[e];
+                    const A av = vs[e];
 #pragma unroll
                     for (int c = 0; c < C; ++c) acc[c] = fma(av, xs[e * C + c], acc[c]);
                 }
                 const int r = d.x + i;
                 if constexpr (kFused) {
-                    epilogue_row(ep, r, acc[0], sq_t, sq_out, dot, mx_t, mx_out, nonfin);
+                    epilogue_row(ep, r, static_cast<double>(acc[0]), sq_t, sq_out, dot, mx_t,
+                                 mx_out, nonfin);
                 } else {
 #pragma unroll
                     for (int c = 0; c < C; ++c)
-                        if (c < ncols) y[r + c * ldy] = acc[c];
+                        if (c < ncols) y[r + c * ldy] = static_cast<double>(acc[c]);
                 }
             }
             // rows longer than kSeqMax (fewer than E / kSeqMax of them): listed
@@ -267,16 +290,17 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                 const bool mine = w0 + g < nw;
                 const int i = mine ? wl[w0 + g] : 0;
                 const int b0 = mine ? ro[i] : 0, b1 = mine ? ro[i + 1] : 0;
-                double acc = 0.0;
+                A acc = 0;
                 for (int e = b0 + gl; e < b1; e += 8) acc = fma(vs[e], xs[e], acc);
 #pragma unroll
                 for (int o = 4; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                 if (mine && gl == 0) {
                     const int r = d.x + i;
                     if constexpr (kFused) {
-                        epilogue_row(ep, r, acc, sq_t, sq_out, dot, mx_t, mx_out, nonfin);
+                        epilogue_row(ep, r, static_cast<double>(acc), sq_t, sq_out, dot, mx_t,
+                                     mx_out, nonfin);
                     } else {
-                        y[r] = acc;
+                        y[r] = static_cast<double>(acc);
                     }
                 }
             }

@@ -19,6 +19,7 @@ public:
     int rows() const override { return rows_; }
     int cols() const override { return cols_; }
     int kind() const override { return column_major_ ? 2 : 1; }
+    const double* values() const { return a_; }
     void apply(const double* x, int block_cols, double* y, cudaStream_t s) const override;
     void apply_transpose(const double* y, int block_cols, double* x,
                          cudaStream_t s) const override;

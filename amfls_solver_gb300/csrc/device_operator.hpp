@@ -69,6 +69,27 @@ struct Epilogue {
     unsigned* counter = nullptr;
 };
 
+// Storage precision of an operator's values.
+enum class ValueType { fp64 = 0, fp32 = 1, bf16 = 2 };
+
+// Validation model of a matrix whose entries are those of a source matrix
+// rounded once to `type` (relative change at most u_t: 2^-24 FP32, 2^-8
+// BF16), with products that round x to FP32 and accumulate in FP32.  The
+// norm bounds widen by the factor (1 +- u_t); the rounding-step counts are
+// expressed in units of the FP64 unit roundoff 2^-53 that the validation
+// formulas use: an FP32 step is 2^29 FP64 steps, and the rounding of x adds
+// one step.
+inline ValidationModel reduced_model(const ValidationModel& m, ValueType type) {
+    const double u = type == ValueType::bf16 ? 0x1p-8 : 0x1p-24;
+    ValidationModel r;
+    r.norm_upper = m.norm_upper * (1.0 + 2.0 * u);
+    r.norm_lower = m.norm_lower * (1.0 - 2.0 * u);
+    constexpr long long kScale = 1LL << 29;
+    r.apply_steps = (m.apply_steps + 1) * kScale;
+    r.transpose_steps = (m.transpose_steps + 1) * kScale;
+    return r;
+}
+
 class DeviceOperator {
 public:
     virtual ~DeviceOperator() = default;

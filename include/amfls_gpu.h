@@ -145,6 +145,40 @@ int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
                                amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
                                int trace_capacity, void* stream);
 
+/* Mixed-precision form (no counterpart in the reference, whose solver is
+ * FP64 throughout).
+ *
+ * amfls_gpu_reduced_operator_create: the matrix of a CSR or dense operator
+ * made by amfls_gpu_csr_operator_create / amfls_gpu_dense_operator_create,
+ * with its values rounded once (to nearest) to FP32 (value_type 1) or BF16
+ * (value_type 2).  Products round x to FP32 and accumulate in FP32; the
+ * operator takes and returns FP64 blocks like any other.  A CSR reduced
+ * operator shares the source's index arrays: destroy it before the source.
+ * Its validation model describes the rounded matrix (norm bounds widened by
+ * the rounding, rounding steps counted in FP64 units: one FP32 step = 2^29).
+ */
+#define AMFLS_GPU_VALUES_FP32 1
+#define AMFLS_GPU_VALUES_BF16 2
+int amfls_gpu_reduced_operator_create(const amfls_gpu_operator* source, int value_type,
+                                      void* stream, amfls_gpu_operator** out);
+
+/* amfls_gpu_solve_amfls_mixed: solve_amfls's problem on `op` (FP64) by
+ * iterative refinement: each outer step runs AMFLS with lambda = 0 to
+ * inner_tolerance on `reduced` (lambda = 0) or on [reduced; sqrt(lambda) I]
+ * (lambda > 0) for the correction of the current x, then validates x with
+ * the certified FP64 validation on `op`.  It stops when that certificate
+ * meets options->tolerance (status 0), when it no longer halves, or after
+ * maximum_refinements steps.  result->status / stop_reason and the metrics
+ * are those of the last FP64 validation; depth and iterations add up the
+ * inner solves; one trace row per outer step (column 0 the step, column 3
+ * the inner basis rank).  Same buffer conventions as amfls_gpu_solve_amfls. */
+int amfls_gpu_solve_amfls_mixed(const amfls_gpu_operator* op, const amfls_gpu_operator* reduced,
+                                const double* d_b, const amfls_gpu_options* options,
+                                double inner_tolerance, int maximum_refinements,
+                                double* d_solution, amfls_gpu_result* result,
+                                double* trace_float, int64_t* trace_int, int trace_capacity,
+                                void* stream);
+
 /* x = A^T y for a row-major dense A (rows x cols) without any device
  * allocation.  No counterpart in the reference: this is for callers that
  * cannot call cudaMalloc (code running during CUDA stream capture, real-time

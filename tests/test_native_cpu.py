@@ -69,3 +69,17 @@ def test_status_constants_match_reference():
     for name, value in [("SUCCESS", 0), ("WORK_LIMIT", 1), ("BASIS_LIMIT", 2),
                         ("PRECISION_LIMIT", 3), ("NUMERICAL_BREAKDOWN", 4)]:
         assert re.search(rf"AMFLS_STATUS_{name} = {value}\b", text)
+
+
+def test_mixed_entry_points_reject_bad_arguments(lib):
+    handle = ctypes.c_void_p()
+    rc = lib.amfls_gpu_reduced_operator_create(None, 3, None, ctypes.byref(handle))
+    assert rc == 1 and b"FP32 (1) or BF16 (2)" in lib.amfls_gpu_last_error()
+    rc = lib.amfls_gpu_reduced_operator_create(None, 1, None, ctypes.byref(handle))
+    assert rc == 1 and b"operator must not be null" in lib.amfls_gpu_last_error()
+    assert handle.value is None
+    res = _native.Result()
+    o = _native.default_options()
+    rc = lib.amfls_gpu_solve_amfls_mixed(None, None, None, ctypes.byref(o), 1e-6, 4, None,
+                                         ctypes.byref(res), None, None, 0, None)
+    assert rc == 1 and b"operator must not be null" in lib.amfls_gpu_last_error()
