@@ -52,7 +52,15 @@ EXPORTED = [
     "amfls_gpu_operator_validation_error_model", "amfls_gpu_solve_amfls",
     "amfls_gpu_solve_fixed_rbgk", "amfls_gpu_dense_apply_transpose_noalloc",
     "amfls_gpu_reduced_operator_create", "amfls_gpu_solve_amfls_mixed",
+    "amfls_gpu_policy_initial_params", "amfls_gpu_policy_create", "amfls_gpu_policy_destroy",
+    "amfls_gpu_policy_forward", "amfls_gpu_policy_gradient", "amfls_gpu_policy_train",
+    "amfls_gpu_solve_amfls_controlled",
 ]
+
+POLICY_FEATURES = 11
+POLICY_INPUTS = 12
+POLICY_PARAMS = 1505
+DECISION_COLUMNS = 15
 
 
 class NativeError(RuntimeError):
@@ -96,6 +104,16 @@ def load():
     lib.amfls_gpu_reduced_operator_create.argtypes = [P, I, P, ctypes.POINTER(P)]
     lib.amfls_gpu_solve_amfls_mixed.argtypes = [P, P, P, ctypes.POINTER(Options), D, I, P,
                                                 ctypes.POINTER(Result), P, P, I, P]
+    U64 = ctypes.c_uint64
+    lib.amfls_gpu_policy_initial_params.argtypes = [U64, P, I]
+    lib.amfls_gpu_policy_create.argtypes = [P, I, ctypes.POINTER(P)]
+    lib.amfls_gpu_policy_destroy.argtypes = [P]
+    lib.amfls_gpu_policy_forward.argtypes = [P, I, P, I, P, P]
+    lib.amfls_gpu_policy_gradient.argtypes = [P, I, P, P, I, P, P, P]
+    lib.amfls_gpu_policy_train.argtypes = [P, I, P, P, I, I, D, P, P, P]
+    lib.amfls_gpu_solve_amfls_controlled.argtypes = [P, P, ctypes.POINTER(Options), P, D, U64,
+                                                     P, I, P, P, ctypes.POINTER(Result), P, P,
+                                                     I, P]
     _lib = lib
     return lib
 

@@ -3,6 +3,7 @@
 // (std::invalid_argument, std::length_error, std::logic_error, ...).
 #include <cstring>
 #include <memory>
+#include <vector>
 #include <stdexcept>
 #include <string>
 
@@ -12,9 +13,14 @@
 #include "csr_operator.hpp"
 #include "dense_operator.hpp"
 #include "reduced_operator.hpp"
+#include "width_policy.hpp"
 
 struct amfls_gpu_operator {
     std::unique_ptr<amfls_gpu::DeviceOperator> impl;
+};
+
+struct amfls_gpu_policy {
+    std::unique_ptr<amfls_gpu::WidthPolicy> impl;
 };
 
 namespace {
@@ -257,6 +263,117 @@ int amfls_gpu_solve_amfls_mixed(const amfls_gpu_operator* op, const amfls_gpu_op
                                                     maximum_refinements, d_solution,
                                                     as_stream(stream));
         export_result(r, result, trace_float, trace_int, trace_capacity);
+    });
+}
+
+static_assert(amfls_gpu::kPolicyParams == AMFLS_GPU_POLICY_PARAMS, "policy size");
+static_assert(amfls_gpu::kPolicyInputs == AMFLS_GPU_POLICY_INPUTS, "policy inputs");
+static_assert(amfls_gpu::kPolicyFeatures == AMFLS_GPU_POLICY_FEATURES, "policy features");
+static_assert(AMFLS_GPU_DECISION_COLUMNS == AMFLS_GPU_POLICY_FEATURES + 4, "decision row");
+
+namespace {
+std::vector<double> policy_params(const double* params, int count) {
+    if (params == nullptr || count != AMFLS_GPU_POLICY_PARAMS)
+        throw std::invalid_argument("policy parameters must be AMFLS_GPU_POLICY_PARAMS doubles");
+    return std::vector<double>(params, params + count);
+}
+void check_batch(const double* inputs, int n) {
+    if (inputs == nullptr || n <= 0) throw std::invalid_argument("policy batch is empty");
+}
+}  // namespace
+
+int amfls_gpu_policy_initial_params(uint64_t seed, double* params, int count) {
+    return guarded([&] {
+        if (params == nullptr || count != AMFLS_GPU_POLICY_PARAMS)
+            throw std::invalid_argument("policy parameters must be AMFLS_GPU_POLICY_PARAMS doubles");
+        const auto p = amfls_gpu::policy_initial_params(seed);
+        std::memcpy(params, p.data(), sizeof(double) * p.size());
+    });
+}
+
+int amfls_gpu_policy_create(const double* params, int count, amfls_gpu_policy** out) {
+    return guarded([&] {
+        if (out == nullptr) throw std::invalid_argument("output handle must not be null");
+        *out = nullptr;
+        auto h = std::make_unique<amfls_gpu_policy>();
+        h->impl = std::make_unique<amfls_gpu::WidthPolicy>(policy_params(params, count));
+        *out = h.release();
+    });
+}
+
+int amfls_gpu_policy_destroy(amfls_gpu_policy* policy) {
+    return guarded([&] { delete policy; });
+}
+
+int amfls_gpu_policy_forward(const double* params, int count, const double* inputs, int n,
+                             double* out, void* stream) {
+    return guarded([&] {
+        check_batch(inputs, n);
+        if (out == nullptr) throw std::invalid_argument("output must not be null");
+        amfls_gpu::policy_forward(policy_params(params, count), inputs, n, out, as_stream(stream));
+    });
+}
+
+int amfls_gpu_policy_gradient(const double* params, int count, const double* inputs,
+                              const double* targets, int n, double* grad, double* loss,
+                              void* stream) {
+    return guarded([&] {
+        check_batch(inputs, n);
+        if (targets == nullptr || grad == nullptr || loss == nullptr)
+            throw std::invalid_argument("targets, grad and loss must not be null");
+        *loss = amfls_gpu::policy_gradient(policy_params(params, count), inputs, targets, n, grad,
+                                           as_stream(stream));
+    });
+}
+
+int amfls_gpu_policy_train(double* params, int count, const double* inputs, const double* targets,
+                           int n, int epochs, double learning_rate, double* loss_first,
+                           double* loss_last, void* stream) {
+    return guarded([&] {
+        check_batch(inputs, n);
+        if (targets == nullptr) throw std::invalid_argument("targets must not be null");
+        auto p = policy_params(params, count);
+        const auto r = amfls_gpu::policy_train(p, inputs, targets, n, epochs, learning_rate,
+                                               as_stream(stream));
+        std::memcpy(params, p.data(), sizeof(double) * p.size());
+        if (loss_first) *loss_first = r.loss_first;
+        if (loss_last) *loss_last = r.loss_last;
+    });
+}
+
+int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double* d_b,
+                                     const amfls_gpu_options* options,
+                                     const amfls_gpu_policy* policy, double exploration,
+                                     uint64_t exploration_seed, double* decisions,
+                                     int decision_capacity, int* decision_rows,
+                                     double* d_solution, amfls_gpu_result* result,
+                                     double* trace_float, int64_t* trace_int, int trace_capacity,
+                                     void* stream) {
+    return guarded([&] {
+        if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
+        if (!(exploration >= 0.0 && exploration <= 1.0))
+            throw std::invalid_argument("exploration must lie in [0, 1]");
+        if (decision_capacity < 0 || (decision_capacity > 0 && decisions == nullptr))
+            throw std::invalid_argument("decision log buffer is invalid");
+        std::vector<amfls_gpu::DecisionRecord> log;
+        amfls_gpu::WidthControl ctl;
+        ctl.policy = policy && policy->impl ? policy->impl.get() : nullptr;
+        ctl.exploration = exploration;
+        ctl.exploration_seed = exploration_seed;
+        ctl.log = &log;
+        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, to_options(options), d_solution,
+                                              as_stream(stream), &ctl);
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+        const int rows = std::min<int>(decision_capacity, (int)log.size());
+        for (int i = 0; i < rows; ++i) {
+            double* row = decisions + (long long)i * AMFLS_GPU_DECISION_COLUMNS;
+            for (int j = 0; j < amfls_gpu::kPolicyFeatures; ++j) row[j] = log[i].features[j];
+            row[11] = log[i].action;
+            row[12] = log[i].heuristic;
+            row[13] = log[i].rate;
+            row[14] = log[i].valid;
+        }
+        if (decision_rows) *decision_rows = (int)log.size();
     });
 }
 

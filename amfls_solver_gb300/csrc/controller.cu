@@ -535,8 +535,47 @@ void absorb_search_counters(const DevState& st, Statistics& s, long long& seen_a
 
 }  // namespace
 
+// Features of a width decision, all from the controller's own state and
+// scaled to order one (their meaning is fixed: a trained policy depends on
+// it):
+//   0 log10(certificate / tol), clipped to [-2, 20]
+//   1 recent certificate decrease per level, decades (0..5)
+//   2 log10 operator seconds per level, clipped to [-7, 1]
+//   3 log10 local (orthogonalisation) seconds per level, clipped to [-7, 1]
+//   4 log10 of the relative block cost of the widened over the current width
+//   5 log2(1 + current width), 6 log2(1 + increment)
+//   7 free basis fraction, 8 free depth fraction
+//   9 a matched-horizon plan is active (0/1), 10 the heuristic widens (0/1)
+void width_features(double* f, double cert, double tol, const History& h, const Plan& plan,
+                    double cost_now, double cost_wide, int frontier, int inc, int rank,
+                    int limit, int depth, int max_depth, bool horizon, bool heuristic) {
+    auto clip = [](double v, double lo, double hi) {
+        return std::isfinite(v) ? std::min(hi, std::max(lo, v)) : (v > 0 ? hi : lo);
+    };
+    f[0] = clip(std::log10(cert / tol), -2.0, 20.0);
+    double lvl = 0.0, op = kInf, loc = kInf;
+    if (h.count > 0) {
+        lvl = h.level_contr[h.count - 1] / std::log(10.0);
+        op = h.op_s[h.count - 1];
+        loc = h.local_s[h.count - 1];
+    } else if (plan.count > 0) {
+        op = plan.op_s[plan.count - 1];
+        loc = plan.local_s[plan.count - 1];
+    }
+    f[1] = clip(lvl, 0.0, 5.0);
+    f[2] = clip(std::log10(op), -7.0, 1.0);
+    f[3] = clip(std::log10(loc), -7.0, 1.0);
+    f[4] = clip(std::log10(cost_wide / cost_now), -3.0, 3.0);
+    f[5] = std::log2(1.0 + frontier);
+    f[6] = std::log2(1.0 + inc);
+    f[7] = limit > 0 ? (double)(limit - rank) / limit : 0.0;
+    f[8] = max_depth > 0 ? (double)(max_depth - depth) / max_depth : 0.0;
+    f[9] = horizon ? 1.0 : 0.0;
+    f[10] = heuristic ? 1.0 : 0.0;
+}
+
 SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const SolveOptions& o,
-                        double* d_solution, cudaStream_t stream) {
+                        double* d_solution, cudaStream_t stream, const WidthControl* control) {
     check_common(op, d_b, o);
     if (o.maximum_epochs < 0 || o.maximum_depth < 0 || o.maximum_auxiliary_width < 0 ||
         o.maximum_basis_size < 0)
@@ -593,7 +632,20 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
         const Candidate c = ev.evaluate(tol, evaluations, aux, result.buffer, best.buffer, &row);
         record(c, train, row);
     };
+    // the open decision record, closed at the next decision or at the end
+    int open_record = -1;
+    double open_cert = kInf, open_time = 0.0;
+    auto close_record = [&]() {
+        if (!control || !control->log || open_record < 0) return;
+        DecisionRecord& r = (*control->log)[open_record];
+        const double now = seconds_since(t_start), cert = certificate(result.v, reg);
+        const double dt = now - open_time;
+        r.rate = (std::log10(open_cert) - std::log10(cert)) / dt;
+        r.valid = std::isfinite(r.rate) && dt > 0.0 ? 1 : 0;
+        open_record = -1;
+    };
     auto finish = [&](const Candidate& c, int status, int reason) {
+        close_record();
         out.iterations = ws.depth();
         out.depth = c.depth;
         out.auxiliary_width = c.auxiliary_width;
@@ -677,9 +729,41 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
                                         ws.basis_rank(), ws.basis_limit(), frontier, hist,
                                         op.relative_block_product_cost(frontier),
                                         op.relative_block_product_cost(tw));
-            if (d.candidate) {
+            bool widen = d.candidate;
+            if (control) {
+                DecisionRecord rec{};
+                width_features(rec.features, interval_cert, tol, hist, plan,
+                               op.relative_block_product_cost(frontier),
+                               op.relative_block_product_cost(tw), frontier, inc,
+                               ws.basis_rank(), ws.basis_limit(), ws.depth(), max_depth,
+                               horizon_active, d.candidate);
+                if (control->policy) {
+                    double stay = 0.0, wide = 0.0;
+                    control->policy->score(rec.features, &stay, &wide, stream);
+                    if (std::isfinite(stay) && std::isfinite(wide)) widen = wide > stay;
+                }
+                if (control->exploration > 0.0) {
+                    std::uint64_t st = control->exploration_seed ^ (0x9e3779b97f4a7c15ULL *
+                                                                    (std::uint64_t)(epoch + 1 + 1000 * ws.depth()));
+                    st = (st ^ (st >> 30)) * 0xbf58476d1ce4e5b9ULL;
+                    st = (st ^ (st >> 27)) * 0x94d049bb133111ebULL;
+                    st ^= st >> 31;
+                    const double u = (double)(st >> 11) * 0x1p-53;
+                    if (u < control->exploration) widen = ((st >> 5) & 1u) != 0;
+                }
+                rec.action = widen ? 1 : 0;
+                rec.heuristic = d.candidate ? 1 : 0;
+                if (control->log) {
+                    close_record();
+                    control->log->push_back(rec);
+                    open_record = (int)control->log->size() - 1;
+                    open_cert = interval_cert;
+                    open_time = seconds_since(t_start);
+                }
+            }
+            if (widen) {
                 requested = inc;
-                if (!horizon_active) req_horizon = d.matched_horizon;
+                if (!horizon_active && d.candidate) req_horizon = d.matched_horizon;
             }
         }
         if (horizon_active && ready && requested == 0) plan = Plan{};

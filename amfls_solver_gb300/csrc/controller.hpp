@@ -6,6 +6,7 @@
 
 #include "device_operator.hpp"
 #include "validation.hpp"
+#include "width_policy.hpp"
 
 namespace amfls_gpu {
 
@@ -67,8 +68,22 @@ struct SolveResult {
     std::vector<TraceRow> trace;
 };
 
+// Optional control of the width decisions (no counterpart in the
+// reference): a learned policy that replaces the heuristic's choice, random
+// exploration (with probability `exploration` the choice is a fair coin),
+// and a log of every decision with its features and the certificate's rate
+// of decrease until the next decision.  Without it (or with all fields
+// empty) solve_amfls is the reference's controller.
+struct WidthControl {
+    const WidthPolicy* policy = nullptr;
+    double exploration = 0.0;
+    std::uint64_t exploration_seed = 0;
+    std::vector<DecisionRecord>* log = nullptr;
+};
+
 SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const SolveOptions& options,
-                        double* d_solution, cudaStream_t stream);
+                        double* d_solution, cudaStream_t stream,
+                        const WidthControl* control = nullptr);
 
 SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b,
                              const SolveOptions& options, double* d_solution, cudaStream_t stream);

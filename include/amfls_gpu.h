@@ -179,6 +179,55 @@ int amfls_gpu_solve_amfls_mixed(const amfls_gpu_operator* op, const amfls_gpu_op
                                 double* trace_float, int64_t* trace_int, int trace_capacity,
                                 void* stream);
 
+/* Learned width controller (no counterpart in the reference).
+ *
+ * A policy is an MLP (AMFLS_GPU_POLICY_INPUTS -> 32 -> 32 -> 1, tanh, FP64)
+ * that scores the controller's two choices at each widening decision (the
+ * reference's decision sites, amfls.cpp:319-359): the inputs are the
+ * AMFLS_GPU_POLICY_FEATURES controller features followed by the action
+ * (0 stay, 1 widen); the output predicts how fast the certificate falls
+ * afterwards.  Parameters are AMFLS_GPU_POLICY_PARAMS doubles laid out
+ * W1[32][12] b1[32] W2[32][32] b2[32] w3[32] b3.  Forward, gradient and
+ * training (full-batch Adam on the mean squared error) run as CUDA kernels;
+ * inputs, targets and parameters are host arrays; all are synchronous. */
+#define AMFLS_GPU_POLICY_FEATURES 11
+#define AMFLS_GPU_POLICY_INPUTS 12
+#define AMFLS_GPU_POLICY_PARAMS 1505
+/* one decision-log row: features[11], action, heuristic choice, rate
+ * (decades of certificate per second until the next decision), valid */
+#define AMFLS_GPU_DECISION_COLUMNS 15
+
+typedef struct amfls_gpu_policy amfls_gpu_policy;
+
+int amfls_gpu_policy_initial_params(uint64_t seed, double* params, int count);
+int amfls_gpu_policy_create(const double* params, int count, amfls_gpu_policy** out);
+int amfls_gpu_policy_destroy(amfls_gpu_policy* policy);
+int amfls_gpu_policy_forward(const double* params, int count, const double* inputs, int n,
+                             double* out, void* stream);
+int amfls_gpu_policy_gradient(const double* params, int count, const double* inputs,
+                              const double* targets, int n, double* grad, double* loss,
+                              void* stream);
+int amfls_gpu_policy_train(double* params, int count, const double* inputs, const double* targets,
+                           int n, int epochs, double learning_rate, double* loss_first,
+                           double* loss_last, void* stream);
+
+/* solve_amfls with its width decisions controlled: with a policy the
+ * policy's choice replaces the heuristic's (a non-finite score falls back to
+ * the heuristic); with exploration in (0, 1] each decision is replaced by a
+ * fair coin with that probability (seeded by exploration_seed).  Every
+ * decision is logged to `decisions` (host, decision_capacity rows of
+ * AMFLS_GPU_DECISION_COLUMNS; *decision_rows receives the count, rows beyond
+ * the capacity are dropped).  policy NULL and exploration 0 give the
+ * reference's controller.  Other conventions as amfls_gpu_solve_amfls. */
+int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double* d_b,
+                                     const amfls_gpu_options* options,
+                                     const amfls_gpu_policy* policy, double exploration,
+                                     uint64_t exploration_seed, double* decisions,
+                                     int decision_capacity, int* decision_rows,
+                                     double* d_solution, amfls_gpu_result* result,
+                                     double* trace_float, int64_t* trace_int, int trace_capacity,
+                                     void* stream);
+
 /* x = A^T y for a row-major dense A (rows x cols) without any device
  * allocation.  No counterpart in the reference: this is for callers that
  * cannot call cudaMalloc (code running during CUDA stream capture, real-time
