@@ -4,7 +4,8 @@ Drop-in for the reference's python/amfls package on CUDA tensors:
 ``run_amfls``, ``run_fixed_rbgk``, ``SolveResult``, ``load_library`` and
 ``torch.ops.amfls.run_amfls`` / ``run_fixed_rbgk`` with the reference's schema,
 plus the mixed-precision form ``run_amfls_mixed`` (FP32 / BF16 inner solves
-refined in FP64).
+refined in FP64), batched solves ``run_amfls_batch`` and, in
+``amfls_solver_gb300.learned``, the learned width controller.
 The compute path is the native library libamfls_gb300.so (C ABI in
 include/amfls_gpu.h); importing this package never falls back to the CPU.
 """
@@ -14,6 +15,7 @@ from .binding import (
     load_library,
     register_torch_ops,
     run_amfls,
+    run_amfls_batch,
     run_amfls_mixed,
     run_fixed_rbgk,
 )
@@ -24,6 +26,7 @@ __all__ = [
     "load_library",
     "register_torch_ops",
     "run_amfls",
+    "run_amfls_batch",
     "run_amfls_mixed",
     "run_fixed_rbgk",
 ]

@@ -54,7 +54,7 @@ EXPORTED = [
     "amfls_gpu_reduced_operator_create", "amfls_gpu_solve_amfls_mixed",
     "amfls_gpu_policy_initial_params", "amfls_gpu_policy_create", "amfls_gpu_policy_destroy",
     "amfls_gpu_policy_forward", "amfls_gpu_policy_gradient", "amfls_gpu_policy_train",
-    "amfls_gpu_solve_amfls_controlled",
+    "amfls_gpu_solve_amfls_controlled", "amfls_gpu_solve_amfls_batch",
 ]
 
 POLICY_FEATURES = 11
@@ -111,6 +111,8 @@ def load():
     lib.amfls_gpu_policy_forward.argtypes = [P, I, P, I, P, P]
     lib.amfls_gpu_policy_gradient.argtypes = [P, I, P, P, I, P, P, P]
     lib.amfls_gpu_policy_train.argtypes = [P, I, P, P, I, I, D, P, P, P]
+    lib.amfls_gpu_solve_amfls_batch.argtypes = [I, P, P, ctypes.POINTER(Options), P,
+                                                ctypes.POINTER(Result), P, I, P]
     lib.amfls_gpu_solve_amfls_controlled.argtypes = [P, P, ctypes.POINTER(Options), P, D, U64,
                                                      P, I, P, P, ctypes.POINTER(Result), P, P,
                                                      I, P]

@@ -289,6 +289,59 @@ def _uint64(v: int) -> int:
     return int(v) & (2**64 - 1)
 
 
+def run_amfls_batch(problems, *, workers: int = 16, regularization=0.0, tolerance=1e-8,
+                    failure_probability: float = 1e-6, maximum_epochs: int = 0,
+                    maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
+                    maximum_basis_size: int = 0, seed: int = 0, stream: int = 0):
+    """Solve many independent problems concurrently on the current GPU.
+
+    `problems` is a sequence of (matrix, b) with matrix a CUDA tensor or a
+    DeviceOperator; `regularization` and `tolerance` may be scalars or one
+    value per problem.  Returns (results, seconds, wall_seconds): a
+    SolveResult per problem (empty traces), each problem's wall time and the
+    batch's.  No counterpart in the reference."""
+    problems = list(problems)
+    count = len(problems)
+    ops = [m if isinstance(m, DeviceOperator) else DeviceOperator(m) for m, _ in problems]
+    bs = [b.contiguous() for _, b in problems]
+    for op, b in zip(ops, bs):
+        if b.device != op.device or b.dtype != torch.float64 or b.numel() != op.rows:
+            raise ValueError("each b must be a float64 CUDA vector of its matrix's row count")
+    def per(v):
+        return list(v) if np.ndim(v) else [v] * count
+    regs, tols = per(regularization), per(tolerance)
+    opts = (_native.Options * max(1, count))()
+    for i in range(count):
+        o = _native.default_options()
+        o.regularization = float(regs[i])
+        o.tolerance = float(tols[i])
+        o.failure_probability = float(failure_probability)
+        o.maximum_epochs = int(maximum_epochs)
+        o.maximum_depth = int(maximum_depth)
+        o.maximum_auxiliary_width = int(maximum_auxiliary_width)
+        o.maximum_basis_size = int(maximum_basis_size)
+        o.seed = _uint64(seed)
+        o.stream = _uint64(stream)
+        opts[i] = o
+    xs = [torch.empty(op.cols, dtype=torch.float64, device=op.device) for op in ops]
+    P = ctypes.c_void_p
+    h_ops = (P * max(1, count))(*[op.handle.value for op in ops])
+    h_b = (P * max(1, count))(*[b.data_ptr() for b in bs])
+    h_x = (P * max(1, count))(*[x.data_ptr() for x in xs])
+    res = (_native.Result * max(1, count))()
+    secs = np.zeros(max(1, count))
+    wall = ctypes.c_double()
+    torch.cuda.synchronize()
+    _native.check(_native.load().amfls_gpu_solve_amfls_batch(
+        count, h_ops, h_b, opts, h_x, res, secs.ctypes.data, int(workers), ctypes.byref(wall)))
+    empty_f, empty_i = torch.zeros((0, 29), dtype=torch.float64), torch.zeros((0, 4), dtype=torch.int64)
+    results = [_decode((xs[i], torch.tensor(list(res[i].metrics), dtype=torch.float64),
+                        torch.tensor(list(res[i].counters), dtype=torch.int64),
+                        torch.tensor(list(res[i].timings), dtype=torch.float64), empty_f, empty_i,
+                        int(res[i].status), int(res[i].stop_reason))) for i in range(count)]
+    return results, secs[:count].copy(), wall.value
+
+
 def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
                     inner_tolerance: float = 1e-6, maximum_refinements: int = 8,
                     regularization: float = 0.0, tolerance: float = 1e-8,

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/amfls_gpu.h"
+#include "batch.hpp"
 #include "common.cuh"
 #include "controller.hpp"
 #include "csr_operator.hpp"
@@ -374,6 +375,35 @@ int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double*
             row[14] = log[i].valid;
         }
         if (decision_rows) *decision_rows = (int)log.size();
+    });
+}
+
+int amfls_gpu_solve_amfls_batch(int count, const amfls_gpu_operator* const* ops,
+                                const double* const* d_b, const amfls_gpu_options* options,
+                                double* const* d_solutions, amfls_gpu_result* results,
+                                double* seconds, int workers, double* wall_seconds) {
+    return guarded([&] {
+        if (count < 0) throw std::invalid_argument("count must be nonnegative");
+        if (count > 0 && (ops == nullptr || d_b == nullptr || options == nullptr ||
+                          d_solutions == nullptr || results == nullptr))
+            throw std::invalid_argument("batch arrays must not be null");
+        std::vector<amfls_gpu::BatchItem> items(count);
+        for (int i = 0; i < count; ++i) {
+            items[i].op = &deref(ops[i]);
+            items[i].b = d_b[i];
+            items[i].options = to_options(&options[i]);
+            items[i].x = d_solutions[i];
+        }
+        const auto out = amfls_gpu::solve_amfls_batch(items, workers, wall_seconds);
+        std::string first_error;
+        for (int i = 0; i < count; ++i) {
+            if (seconds) seconds[i] = out[i].seconds;
+            if (out[i].ok)
+                export_result(out[i].result, &results[i], nullptr, nullptr, 0);
+            else if (first_error.empty())
+                first_error = "problem " + std::to_string(i) + ": " + out[i].error;
+        }
+        if (!first_error.empty()) throw std::runtime_error(first_error);
     });
 }
 

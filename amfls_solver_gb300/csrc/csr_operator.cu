@@ -28,6 +28,7 @@
 #include <memory>
 #include <stdexcept>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -342,20 +343,21 @@ __global__ void rows_major_kernel(const double* __restrict__ x, long long ld, in
 // tiles), at most one warp per tile and at most kMaxBlocks CTAs.
 template <typename V, int C, int E, bool kFused>
 int tile_grid(int ntiles) {
-    static int per_sm = -1, sms = 0;
-    if (per_sm < 0) {
+    // resident CTAs per SM and SM count, set up once per instantiation (a
+    // function-local static is initialised once even with concurrent callers)
+    static const std::pair<int, int> occ = [] {
         constexpr int bytes = csr_tiles::smem_bytes<C, E>();
         AMFLS_CUDA(cudaFuncSetAttribute(csr_tiles::tile_product_kernel<V, C, E, kFused>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-        int dev = 0, nb = 0;
+        int dev = 0, nb = 0, sms = 0;
         AMFLS_CUDA(cudaGetDevice(&dev));
         AMFLS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &nb, csr_tiles::tile_product_kernel<V, C, E, kFused>, csr_tiles::kThreads, bytes));
-        per_sm = std::max(1, nb);
-    }
+        return std::make_pair(std::max(1, nb), sms);
+    }();
     const int need = (ntiles + csr_tiles::kWarps - 1) / csr_tiles::kWarps;
-    return std::max(1, std::min({need, per_sm * sms, kMaxBlocks}));
+    return std::max(1, std::min({need, occ.first * occ.second, kMaxBlocks}));
 }
 
 template <int C, bool kFused, typename V>

@@ -166,6 +166,29 @@ def scaled_dense(m: int, n: int, decades: float = 6.0, seed: int = 0,
     return DenseProblem(g, b)
 
 
+def uneven_csr_batch(count: int = 256, seed: int = 0, m_range=(2_000, 200_000),
+                     n_range=(500, 50_000), per_row=(5, 40), cond_range=(1e3, 1e8),
+                     reg_range=(1e-8, 1e-2), tolerance: float = 1e-9, noise: float = 1e-8):
+    """Independent CSR least-squares problems of uneven size: m and n
+    log-uniform (n <= 2 m), 5..40 nonzeros per row (uniform per row), N(0,1)
+    values with geometric column scaling to a log-uniform condition, lambda
+    log-uniform; b = A x_true + noise.  Returns [(problem, lambda, tol)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        m = int(np.exp(rng.uniform(np.log(m_range[0]), np.log(m_range[1]))))
+        n = int(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        n = max(1, min(n, 2 * m))
+        decades = float(rng.uniform(np.log10(cond_range[0]), np.log10(cond_range[1])))
+        reg = float(np.exp(rng.uniform(np.log(reg_range[0]), np.log(reg_range[1]))))
+        prng = np.random.default_rng([seed, i])
+        lengths = prng.integers(per_row[0], per_row[1] + 1, size=m)
+        cols = _distinct_columns(prng, lengths, n)
+        prob = _finish_csr(prng, m, n, np.minimum(lengths, n), cols, decades, noise)
+        out.append((prob, reg, tolerance))
+    return out
+
+
 # The named workloads (full sizes).  Each entry gives the generator, its
 # keyword arguments and the solver options.
 WORKLOADS = {

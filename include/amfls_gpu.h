@@ -228,6 +228,20 @@ int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double*
                                      double* trace_float, int64_t* trace_int, int trace_capacity,
                                      void* stream);
 
+/* Batched AMFLS (no counterpart in the reference): `count` independent
+ * problems, problem i = (ops[i], d_b[i], options[i]) with its solution in
+ * d_solutions[i], solved concurrently by `workers` host threads with one
+ * CUDA stream each (streams created and destroyed inside the call),
+ * largest problems (by nonzeros, or rows x cols) first.  results[i] as from
+ * amfls_gpu_solve_amfls (trace rows counted, not copied); seconds[i] (may be
+ * NULL) the wall time of problem i; *wall_seconds (may be NULL) the whole
+ * batch.  Returns the first problem's error if any solve raised (the others
+ * still run); synchronous. */
+int amfls_gpu_solve_amfls_batch(int count, const amfls_gpu_operator* const* ops,
+                                const double* const* d_b, const amfls_gpu_options* options,
+                                double* const* d_solutions, amfls_gpu_result* results,
+                                double* seconds, int workers, double* wall_seconds);
+
 /* x = A^T y for a row-major dense A (rows x cols) without any device
  * allocation.  No counterpart in the reference: this is for callers that
  * cannot call cudaMalloc (code running during CUDA stream capture, real-time
