@@ -47,6 +47,14 @@ std::vector<BatchOutcome> solve_amfls_batch(const std::vector<BatchItem>& items,
     for (const BatchItem& it : items)
         if (it.op == nullptr || it.b == nullptr || it.x == nullptr)
             throw std::invalid_argument("batch problems need an operator, b and a solution buffer");
+    {
+        // an operator's products use scratch it owns: concurrent solves need one each
+        std::vector<const DeviceOperator*> ops;
+        for (const BatchItem& it : items) ops.push_back(it.op);
+        std::sort(ops.begin(), ops.end());
+        if (std::adjacent_find(ops.begin(), ops.end()) != ops.end())
+            throw std::invalid_argument("each problem of a batch needs its own operator");
+    }
     workers = std::min(workers, count);
     std::vector<int> order(count);
     std::iota(order.begin(), order.end(), 0);

@@ -45,19 +45,18 @@ bool truncated_or_broken(const StepAudit& a) {
 }
 
 // Grow a device buffer to hold `need` elements; `keep` elements of the old
-// contents survive.  Synchronises the stream before freeing.
+// contents survive (copy and free are ordered on the stream).
 template <typename T>
 void grow(T*& p, long long& cap, long long need, long long keep, cudaStream_t s) {
     if (need <= cap) return;
     long long c = std::max<long long>(need, cap + cap / 2);
     T* q = nullptr;
-    AMFLS_CUDA(cudaMalloc(&q, sizeof(T) * c));
+    stream_alloc(&q, sizeof(T) * c, s);
     if (p) {
         if (keep > 0)
             AMFLS_CUDA(cudaMemcpyAsync(q, p, sizeof(T) * std::min(keep, cap),
                                        cudaMemcpyDeviceToDevice, s));
-        AMFLS_CUDA(cudaStreamSynchronize(s));
-        cudaFree(p);
+        stream_free(p, s);
     }
     p = q;
     cap = c;
@@ -108,13 +107,13 @@ void Workspace::ensure_u_capacity(int cols) {
     const long long keep = (long long)m_ * (host_.left_width + host_.pending);
     double* u = nullptr;
     double* u2 = nullptr;
-    AMFLS_CUDA(cudaMalloc(&u, sizeof(double) * m_ * (size_t)cap));
-    AMFLS_CUDA(cudaMalloc(&u2, sizeof(double) * m_ * (size_t)cap));
+    stream_alloc(&u, sizeof(double) * m_ * (size_t)cap, stream_);
+    stream_alloc(&u2, sizeof(double) * m_ * (size_t)cap, stream_);
     if (keep > 0)
         AMFLS_CUDA(cudaMemcpyAsync(u, U_, sizeof(double) * keep, cudaMemcpyDeviceToDevice, stream_));
     AMFLS_CUDA(cudaStreamSynchronize(stream_));
-    cudaFree(U_);
-    cudaFree(U2_);
+    stream_free(U_, stream_);
+    stream_free(U2_, stream_);
     U_ = u;
     U2_ = u2;
     ucap_ = cap;
@@ -126,23 +125,23 @@ void Workspace::ensure_block_capacity(int width) {
         const int cap = std::max(width, 2 * bcap_);
         AMFLS_CUDA(cudaStreamSynchronize(stream_));
         for (double** p : {&BR_, &BL_, &BQ_, &BT_}) {
-            cudaFree(*p);
+            stream_free(*p, stream_);
             *p = nullptr;
         }
         const size_t rows_max = std::max(m_, n_);
-        AMFLS_CUDA(cudaMalloc(&BR_, sizeof(double) * n_ * (size_t)cap));
-        AMFLS_CUDA(cudaMalloc(&BL_, sizeof(double) * m_ * (size_t)cap));
-        AMFLS_CUDA(cudaMalloc(&BQ_, sizeof(double) * n_ * (size_t)cap));
-        AMFLS_CUDA(cudaMalloc(&BT_, sizeof(double) * rows_max * (size_t)cap));
+        stream_alloc(&BR_, sizeof(double) * n_ * (size_t)cap, stream_);
+        stream_alloc(&BL_, sizeof(double) * m_ * (size_t)cap, stream_);
+        stream_alloc(&BQ_, sizeof(double) * n_ * (size_t)cap, stream_);
+        stream_alloc(&BT_, sizeof(double) * rows_max * (size_t)cap, stream_);
         bcap_ = cap;
     }
     const long long c = std::max(width, 1);
     grow(small_, small_cap_, 10 * c * c + 8 * c + jacobi_work_doubles((int)c) + 256, 0, stream_);
     if (!dflags_) {
-        AMFLS_CUDA(cudaMalloc(&dflags_, sizeof(int) * 8));
+        stream_alloc(&dflags_, sizeof(int) * 8, stream_);
         AMFLS_CUDA(cudaMemsetAsync(dflags_, 0, sizeof(int) * 8, stream_));
     }
-    if (!dnorm_) AMFLS_CUDA(cudaMalloc(&dnorm_, sizeof(NormResult)));
+    if (!dnorm_) stream_alloc(&dnorm_, sizeof(NormResult), stream_);
     if (!ev_[0]) {
         AMFLS_CUDA(cudaEventCreate(&ev_[0]));
         AMFLS_CUDA(cudaEventCreate(&ev_[1]));

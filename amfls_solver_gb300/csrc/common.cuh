@@ -36,6 +36,24 @@ inline long long& launch_count() {
         ++::amfls_gpu::launch_count();                               \
     } while (0)
 
+// Stream-ordered device allocation from the device's default memory pool.
+// A solve allocates and frees its buffers on its own stream: unlike
+// cudaFree, cudaFreeAsync does not synchronise the whole device, so solves
+// running concurrently on different streams do not stall each other.
+template <typename T>
+inline void stream_alloc(T** p, size_t bytes, cudaStream_t s) {
+    check_cuda(cudaMallocAsync(reinterpret_cast<void**>(p), bytes, s), "cudaMallocAsync");
+}
+inline void stream_free(const void* p, cudaStream_t s) {
+    if (p) cudaFreeAsync(const_cast<void*>(p), s);
+}
+
+// Keeps freed blocks of the current device's default memory pool cached in
+// the process (release threshold = unlimited) instead of returning them to
+// the driver at every synchronisation, so consecutive solves reuse their
+// buffers.  Called by each solve; takes effect once per device.
+void keep_pool_memory();
+
 constexpr int kWarp = 32;
 constexpr int kPanel = 32;  // columns per V panel (row-major n x 32 tiles)
 

@@ -429,11 +429,11 @@ public:
     Evaluator(Workspace& ws, const DeviceOperator& op, const double* d_b, double reg,
               Statistics& stats, cudaStream_t stream)
         : ws_(ws), validator_(op, d_b, reg, stream), stats_(stats), stream_(stream), n_(op.cols()) {
-        for (auto& p : buf_) AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * std::max(1, n_)));
+        for (auto& p : buf_) stream_alloc(&p, sizeof(double) * std::max(1, n_), stream_);
     }
     ~Evaluator() {
         cudaStreamSynchronize(stream_);
-        for (auto p : buf_) cudaFree(p);
+        for (auto p : buf_) stream_free(p, stream_);
     }
 
     Candidate evaluate(double tol, int epoch, int aux, int keep_a, int keep_b, TraceRow* row) {

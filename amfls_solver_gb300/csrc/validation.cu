@@ -609,25 +609,25 @@ struct Validator::Impl {
         : op(o), b(bb), reg(rg), stream(s), m(o.rows()), n(o.cols()) {
         const ValidationModel vm = op.validation_error_model();
         mdl = {vm.norm_upper, vm.norm_lower, vm.apply_steps, vm.transpose_steps};
-        AMFLS_CUDA(cudaMalloc(&vs, sizeof(ValState)));
+        stream_alloc(&vs, sizeof(ValState), stream);
         auto alloc = [&](double*& p, long long cnt) {
-            AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * std::max<long long>(1, cnt)));
+            stream_alloc(&p, sizeof(double) * std::max<long long>(1, cnt), stream);
         };
         alloc(ax, m);
         alloc(r, m);
         alloc(atr, n);
         alloc(g, n);
         alloc(partials, 2 * kMaxVectors * 1216 + 8 * 1216);
-        AMFLS_CUDA(cudaMalloc(&counters, sizeof(unsigned) * 16));
+        stream_alloc(&counters, sizeof(unsigned) * 16, stream);
         AMFLS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned) * 16, stream));
         AMFLS_CUDA(cudaEventCreate(&ev[0]));
         AMFLS_CUDA(cudaEventCreate(&ev[1]));
     }
     ~Impl() {
         cudaStreamSynchronize(stream);
-        for (double* p : {ax, r, atr, g, hi1, lo1, hi2, lo2, rn_hi, rn_lo, g2, partials}) cudaFree(p);
-        cudaFree(vs);
-        cudaFree(counters);
+        for (double* p : {ax, r, atr, g, hi1, lo1, hi2, lo2, rn_hi, rn_lo, g2, partials}) stream_free(p, stream);
+        stream_free(vs, stream);
+        stream_free(counters, stream);
         cudaEventDestroy(ev[0]);
         cudaEventDestroy(ev[1]);
     }
@@ -703,7 +703,7 @@ struct Validator::Impl {
         const double* grad = g;
         if (h.need_refine) {
             auto alloc = [&](double*& p, long long cnt) {
-                if (!p) AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * std::max<long long>(1, cnt)));
+                if (!p) stream_alloc(&p, sizeof(double) * std::max<long long>(1, cnt), stream);
             };
             alloc(hi1, m);
             alloc(lo1, m);

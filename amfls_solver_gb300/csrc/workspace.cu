@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
 #include <vector>
 
@@ -31,6 +32,20 @@
 #include "workspace.hpp"
 
 namespace amfls_gpu {
+
+void keep_pool_memory() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    AMFLS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || done[dev]) return;
+    cudaMemPool_t pool;
+    AMFLS_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    unsigned long long threshold = ~0ULL;
+    AMFLS_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+    done[dev] = true;
+}
 
 namespace {
 
@@ -560,13 +575,13 @@ PanelStore::PanelStore(int n, int max_panels, cudaStream_t stream)
     : n_(n), stream_(stream), table_cap_(std::max(1, max_panels)) {
     // fixed-capacity device table: its address never changes, so captured
     // kernels may keep it
-    AMFLS_CUDA(cudaMalloc(&table_, sizeof(double*) * table_cap_));
+    stream_alloc(&table_, sizeof(double*) * table_cap_, stream_);
     host_.reserve(table_cap_);
 }
 
 PanelStore::~PanelStore() {
-    for (double* p : host_) cudaFree(p);
-    cudaFree(table_);
+    for (double* p : host_) stream_free(p, stream_);
+    stream_free(table_, stream_);
 }
 
 void PanelStore::ensure_columns(int cols) {
@@ -576,7 +591,7 @@ void PanelStore::ensure_columns(int cols) {
     const int first = panels();
     while (panels() < need) {
         double* p = nullptr;
-        AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * 32 * static_cast<size_t>(n_)));
+        stream_alloc(&p, sizeof(double) * 32 * static_cast<size_t>(n_), stream_);
         AMFLS_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * 32 * static_cast<size_t>(n_), stream_));
         host_.push_back(p);
     }
@@ -598,24 +613,25 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     if (!std::isfinite(regularization) || regularization < 0.0)
         throw std::invalid_argument("block Golub-Kahan regularization must be finite and nonnegative");
     if (maximum_basis_size < 0) throw std::invalid_argument("block Golub-Kahan basis limit must be nonnegative");
+    keep_pool_memory();
     const int mn = std::min(m_, n_);
     basis_limit_ = maximum_basis_size > 0 ? std::min(maximum_basis_size, mn) : mn;
-    AMFLS_CUDA(cudaMalloc(&dstate_, sizeof(DevState)));
-    AMFLS_CUDA(cudaMalloc(&red_, sizeof(RedResult) * 4));
+    stream_alloc(&dstate_, sizeof(DevState), stream_);
+    stream_alloc(&red_, sizeof(RedResult) * 4, stream_);
     // scratch: V^T r partials ((target blocks + panels) x 32), then the
     // per-block norm partials of the V c sweep (n/32 + slack)
     const long long max_panels = basis_limit_ / 32 + 2;
     vc_partials_offset_ = (kGemvTargetBlocks + max_panels) * 32 + 6 * 1216;
     const long long pcount = vc_partials_offset_ + (n_ + 31) / 32 + 1024;
-    AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * pcount));
+    stream_alloc(&partials_, sizeof(double) * pcount, stream_);
     const long long ncounters = 64 + max_panels + 64;
-    AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * ncounters));
+    stream_alloc(&counter_, sizeof(unsigned) * ncounters, stream_);
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * ncounters, stream_));
-    AMFLS_CUDA(cudaMalloc(&R_, sizeof(double) * n_));
-    AMFLS_CUDA(cudaMalloc(&vnew_, sizeof(double) * n_));
-    AMFLS_CUDA(cudaMalloc(&Y_, sizeof(double) * m_));
+    stream_alloc(&R_, sizeof(double) * n_, stream_);
+    stream_alloc(&vnew_, sizeof(double) * n_, stream_);
+    stream_alloc(&Y_, sizeof(double) * m_, stream_);
     ucap_ = 1;
-    AMFLS_CUDA(cudaMalloc(&U_, sizeof(double) * m_ * ucap_));
+    stream_alloc(&U_, sizeof(double) * m_ * ucap_, stream_);
     V_ = std::make_unique<PanelStore>(n_, static_cast<int>(max_panels), stream_);
     V_->ensure_columns(1);  // panel 0 exists (zeroed) before any level runs
     AMFLS_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
@@ -631,39 +647,39 @@ Workspace::~Workspace() {
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
     if (graph_) cudaGraphDestroy(graph_);
     if (capture_stream_) cudaStreamDestroy(capture_stream_);
-    cudaFree(dstate_);
-    cudaFree(red_);
-    cudaFree(partials_);
-    cudaFree(counter_);
-    cudaFree(R_);
-    cudaFree(vnew_);
-    cudaFree(Y_);
-    cudaFree(U_);
-    cudaFree(P_);
-    cudaFree(c1_);
-    cudaFree(c2_);
-    cudaFree(alpha_);
-    cudaFree(beta_);
-    cudaFree(g_);
-    cudaFree(qr_);
-    cudaFree(qr_state_);
-    cudaFree(U2_);
-    cudaFree(BR_);
-    cudaFree(BL_);
-    cudaFree(BQ_);
-    cudaFree(BT_);
-    cudaFree(small_);
-    cudaFree(coefs_);
-    cudaFree(bpart_);
-    cudaFree(tsqr_);
-    cudaFree(dflags_);
-    cudaFree(dnorm_);
-    cudaFree(d_meta_);
-    cudaFree(d_vals_);
-    cudaFree(d_pstate_);
-    cudaFree(d_carry_);
-    cudaFree(d_pwork_);
-    cudaFree(d_y_);
+    stream_free(dstate_, stream_);
+    stream_free(red_, stream_);
+    stream_free(partials_, stream_);
+    stream_free(counter_, stream_);
+    stream_free(R_, stream_);
+    stream_free(vnew_, stream_);
+    stream_free(Y_, stream_);
+    stream_free(U_, stream_);
+    stream_free(P_, stream_);
+    stream_free(c1_, stream_);
+    stream_free(c2_, stream_);
+    stream_free(alpha_, stream_);
+    stream_free(beta_, stream_);
+    stream_free(g_, stream_);
+    stream_free(qr_, stream_);
+    stream_free(qr_state_, stream_);
+    stream_free(U2_, stream_);
+    stream_free(BR_, stream_);
+    stream_free(BL_, stream_);
+    stream_free(BQ_, stream_);
+    stream_free(BT_, stream_);
+    stream_free(small_, stream_);
+    stream_free(coefs_, stream_);
+    stream_free(bpart_, stream_);
+    stream_free(tsqr_, stream_);
+    stream_free(dflags_, stream_);
+    stream_free(dnorm_, stream_);
+    stream_free(d_meta_, stream_);
+    stream_free(d_vals_, stream_);
+    stream_free(d_pstate_, stream_);
+    stream_free(d_carry_, stream_);
+    stream_free(d_pwork_, stream_);
+    stream_free(d_y_, stream_);
     for (cudaEvent_t e : ev_)
         if (e) cudaEventDestroy(e);
 }
@@ -675,13 +691,13 @@ void Workspace::ensure_t_capacity(int cols) {
     AMFLS_CUDA(cudaStreamSynchronize(stream_));
     auto grow = [&](double*& p, size_t old_count, size_t new_count) {
         double* q = nullptr;
-        AMFLS_CUDA(cudaMalloc(&q, sizeof(double) * new_count));
+        stream_alloc(&q, sizeof(double) * new_count, stream_);
         AMFLS_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * new_count, stream_));
         if (p) {
             AMFLS_CUDA(cudaMemcpyAsync(q, p, sizeof(double) * old_count, cudaMemcpyDeviceToDevice,
                                        stream_));
             AMFLS_CUDA(cudaStreamSynchronize(stream_));
-            cudaFree(p);
+            stream_free(p, stream_);
         }
         p = q;
     };
@@ -692,10 +708,10 @@ void Workspace::ensure_t_capacity(int cols) {
     grow(c1_, old, cap);
     grow(c2_, old, cap);
     // the QR arrays are laid out by capacity: rebuild them from scratch
-    cudaFree(qr_);
+    stream_free(qr_, stream_);
     qr_ = nullptr;
-    AMFLS_CUDA(cudaMalloc(&qr_, sizeof(double) * 4 * cap));
-    if (!qr_state_) AMFLS_CUDA(cudaMalloc(&qr_state_, sizeof(double) * 8));
+    stream_alloc(&qr_, sizeof(double) * 4 * cap, stream_);
+    if (!qr_state_) stream_alloc(&qr_state_, sizeof(double) * 8, stream_);
     AMFLS_CUDA(cudaMemsetAsync(qr_state_, 0, sizeof(double) * 8, stream_));
     tcap_ = cap;
     ccap_ = cap;

@@ -16,6 +16,13 @@ e2e       the same solve through the public API run_amfls on host tensors:
           construction, solve, device->host copy of the solution;
 spmm      CSR SpMM and SpMM^T GB/s (s = 1 and 8) on the 2,000,000 x 500,000
           power-law matrix, the metric's second half;
+mixed     time-to-tol of the mixed-precision form (FP32 inner solves refined
+          in FP64, certified by the FP64 validation) next to plain FP64 on
+          the 20000 x 5000 CSR problem, and the mixed form on the headline
+          workload;
+batched   problems/s, p50 and p99 per-problem time of batched solves on a
+          bounded sample of the uneven 256-problem CSR workload (sizes as
+          described in the line), 16 workers against 1;
 roofline  the dominant kernel timed live with CUDA events on its stream over
           repeated launches (algorithmic bytes per launch / mean duration);
           for the dense operator the FP64 issue rate, not HBM, is the bound,
@@ -61,6 +68,9 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1, help="0 skips the cpu_baseline leg")
     ap.add_argument("--spmm", type=int, default=1,
                     help="0 skips the CSR SpMM GB/s measurement on the 2M x 500k matrix")
+    ap.add_argument("--mixed", type=int, default=1, help="0 skips the mixed-precision leg")
+    ap.add_argument("--batched", type=int, default=48,
+                    help="problems in the batched leg's sample (0 skips it)")
     return ap.parse_args()
 
 
@@ -144,10 +154,11 @@ CPU_SAMPLE_LEVELS = {"dense_100000x2000": 240, "csr_20000x5000": 768}
 
 
 def algorithmic_bytes(prob):
-    """Bytes one single-column product moves at minimum (int32 indices in HBM)."""
+    """Bytes one single-column product moves at minimum (int32 indices and
+    row offsets in HBM; the mean of A v and A^T u for CSR)."""
     if hasattr(prob, "row_offsets"):
         nnz = prob.nnz
-        return nnz * (8 + 4) + (prob.rows + 1) * 8 + (prob.rows + prob.cols) * 8
+        return nnz * (8 + 4) + (0.5 * (prob.rows + prob.cols) + 1) * 4 + (prob.rows + prob.cols) * 8
     m, n = prob.rows, prob.cols
     return 8 * m * n + 8 * (m + n)
 
@@ -259,6 +270,86 @@ def spmm_measurement(dev, stream, peak):
             res[name] = {"us": t * 1e6, "achieved": nbytes / t / 1e9,
                          "frac": nbytes / t / 1e9 / peak, "algorithmic_bytes": nbytes}
         out[f"s{cols}"] = res
+    return out
+
+
+def mixed_measurement(dev, headline_op, headline_b, headline_opts):
+    """Plain FP64 vs mixed FP32 time-to-tol (host wall clock around the
+    synchronous C-ABI solves, after one warm-up each)."""
+    import torch
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import binding, _native
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    def cert(r, reg):
+        return r.relative_energy_error_upper_bound if reg > 0 else r.backward_error_upper_bound
+
+    out = {}
+    prob, opts = make_workload("csr_20000x5000")
+    a = torch.sparse_csr_tensor(torch.from_numpy(prob.row_offsets),
+                                torch.from_numpy(prob.column_indices),
+                                torch.from_numpy(prob.values), size=(prob.rows, prob.cols)).to(dev)
+    op = amfls.DeviceOperator(a)
+    b = torch.from_numpy(prob.b).to(dev)
+    o = _native.default_options()
+    for k, v in opts.items():
+        setattr(o, k, v)
+    plain, t_plain = timed(lambda: binding._decode(binding._solve_raw("amfls", op, b, o)))
+    low = op.reduced("fp32")
+    mixed, t_mixed = timed(lambda: amfls.run_amfls_mixed(op, b, reduced=low, inner_tolerance=1e-7,
+                                                         maximum_refinements=6, **opts))
+    out["csr_20000x5000"] = {
+        "tolerance": opts["tolerance"],
+        "fp64": {"s": t_plain, "status": plain.status, "depth": plain.depth,
+                 "certificate": cert(plain, 0.0)},
+        "mixed_fp32": {"s": t_mixed, "status": mixed.status, "levels": mixed.depth,
+                       "steps": int(mixed.trace_float.shape[0]), "inner_tolerance": 1e-7,
+                       "certificate": cert(mixed, 0.0),
+                       "x_rel_diff_vs_fp64": float(torch.linalg.norm(mixed.solution - plain.solution)
+                                                   / torch.linalg.norm(plain.solution))},
+        "speedup": t_plain / t_mixed}
+    reg = headline_opts.get("regularization", 0.0)
+    hlow = headline_op.reduced("fp32")
+    hm, t_hm = timed(lambda: amfls.run_amfls_mixed(headline_op, headline_b, reduced=hlow,
+                                                   inner_tolerance=1e-7, maximum_refinements=6,
+                                                   **headline_opts))
+    out["headline"] = {"s": t_hm, "status": hm.status, "levels": hm.depth,
+                       "steps": int(hm.trace_float.shape[0]), "certificate": cert(hm, reg)}
+    return out
+
+
+def batched_measurement(dev, count):
+    """Batched solves of a bounded sample of the uneven CSR workload."""
+    import torch
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import problems
+
+    batch = problems.uneven_csr_batch(count, seed=20251203, m_range=(2_000, 50_000),
+                                      n_range=(500, 12_500))
+    mats = [(amfls.DeviceOperator(torch.sparse_csr_tensor(
+        torch.from_numpy(p.row_offsets), torch.from_numpy(p.column_indices),
+        torch.from_numpy(p.values), size=(p.rows, p.cols)).to(dev)),
+        torch.from_numpy(p.b).to(dev)) for p, _, _ in batch]
+    regs = [r for _, r, _ in batch]
+    out = {"sample": (f"{count} problems of the uneven workload's distribution with m in "
+                      f"[2e3, 5e4] and n in [500, 1.25e4] (the full ranges reach 2e5 x 5e4); "
+                      f"5-40 nonzeros per row, condition 1e3-1e8, lambda 1e-8-1e-2, tol 1e-9"),
+           "nnz": int(sum(p.nnz for p, _, _ in batch))}
+    for workers in (16, 1):
+        res, secs, wall = amfls.run_amfls_batch(mats, workers=workers, regularization=regs,
+                                                tolerance=1e-9)
+        st = [r.status for r in res]
+        out[f"workers_{workers}"] = {
+            "problems_per_s": count / wall, "wall_s": wall,
+            "p50_s": float(np.percentile(secs, 50)), "p99_s": float(np.percentile(secs, 99)),
+            "certified": st.count(0), "levels": int(sum(r.depth for r in res))}
     return out
 
 
@@ -417,7 +508,7 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = measured_peaks()
     nbytes = algorithmic_bytes(prob)
     achieved = nbytes / kt / 1e9
-    roof = {"kernel": ("spmv_binned_kernel" if is_csr else
+    roof = {"kernel": ("tile_product_kernel<double,1,256,fused> (A v, A^T u)" if is_csr else
                        "dot_block_kernel<1> (A^T u) / across_block_kernel<1> (A v)"),
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
@@ -434,6 +525,8 @@ def run_ours(args, world, rank, local):
         roof["fp64"]["frac"] = roof["fp64"]["achieved_tflops"] / roof["fp64"]["dgemm_tflops"]
 
     spmm = spmm_measurement(dev, stream, peak) if args.spmm else None
+    mixed = mixed_measurement(dev, op, b_dev, opts) if args.mixed and rank == 0 else None
+    batched = batched_measurement(dev, args.batched) if args.batched > 0 and rank == 0 else None
 
     if rank != 0:
         return
@@ -454,7 +547,8 @@ def run_ours(args, world, rank, local):
                        "depth": depth, "status": list(status), "parallelism": "replicas"},
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": roof, "spmm": spmm, "cpu_baseline": cpu, "clocks": clocks.summary(),
+            "roofline": roof, "spmm": spmm, "mixed": mixed, "batched": batched,
+            "cpu_baseline": cpu, "clocks": clocks.summary(),
             "gpu_launches": launches * args.steps}
     print(json.dumps(line), flush=True)
 

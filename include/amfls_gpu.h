@@ -230,7 +230,8 @@ int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double*
 
 /* Batched AMFLS (no counterpart in the reference): `count` independent
  * problems, problem i = (ops[i], d_b[i], options[i]) with its solution in
- * d_solutions[i], solved concurrently by `workers` host threads with one
+ * d_solutions[i] (a distinct operator per problem: an operator's products
+ * use scratch it owns), solved concurrently by `workers` host threads with one
  * CUDA stream each (streams created and destroyed inside the call),
  * largest problems (by nonzeros, or rows x cols) first.  results[i] as from
  * amfls_gpu_solve_amfls (trace rows counted, not copied); seconds[i] (may be

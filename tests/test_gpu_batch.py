@@ -40,3 +40,14 @@ def test_batch_reports_bad_problems_without_stopping_the_others():
     good = (csr_tensor(p), torch.from_numpy(p.b).cuda())
     with pytest.raises(RuntimeError, match="problem 1"):
         amfls.run_amfls_batch([good, good], workers=2, tolerance=[1e-8, 2.0])
+
+
+def test_batch_rejects_a_shared_operator():
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import problems
+
+    p = problems.scaled_uniform_csr(3000, 500, seed=2)
+    op = amfls.DeviceOperator(csr_tensor(p))
+    b = torch.from_numpy(p.b).cuda()
+    with pytest.raises(RuntimeError, match="its own operator"):
+        amfls.run_amfls_batch([(op, b), (op, b)], workers=2)
