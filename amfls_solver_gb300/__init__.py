@@ -18,6 +18,7 @@ from .binding import (
     run_amfls_batch,
     run_amfls_mixed,
     run_fixed_rbgk,
+    solve_amfls,
 )
 
 __all__ = [
@@ -29,4 +30,5 @@ __all__ = [
     "run_amfls_batch",
     "run_amfls_mixed",
     "run_fixed_rbgk",
+    "solve_amfls",
 ]

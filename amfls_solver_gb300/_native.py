@@ -43,6 +43,18 @@ class ValidationModel(ctypes.Structure):
                 ("apply_transpose_rounding_steps", ctypes.c_longlong)]
 
 
+APPLY_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                            ctypes.c_void_p, ctypes.c_void_p)
+COST_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_void_p, ctypes.c_int)
+
+
+class Callbacks(ctypes.Structure):
+    _fields_ = [("context", ctypes.c_void_p), ("apply", APPLY_FN),
+                ("apply_transpose", APPLY_FN), ("relative_block_product_cost", COST_FN),
+                ("has_validation_model", ctypes.c_int),
+                ("validation_model", ValidationModel)]
+
+
 # every symbol include/amfls_gpu.h declares
 EXPORTED = [
     "amfls_gpu_default_options", "amfls_gpu_last_error", "amfls_gpu_csr_operator_create",
@@ -55,6 +67,7 @@ EXPORTED = [
     "amfls_gpu_policy_initial_params", "amfls_gpu_policy_create", "amfls_gpu_policy_destroy",
     "amfls_gpu_policy_forward", "amfls_gpu_policy_gradient", "amfls_gpu_policy_train",
     "amfls_gpu_solve_amfls_controlled", "amfls_gpu_solve_amfls_batch",
+    "amfls_gpu_callback_operator_create",
 ]
 
 POLICY_FEATURES = 11
@@ -111,6 +124,8 @@ def load():
     lib.amfls_gpu_policy_forward.argtypes = [P, I, P, I, P, P]
     lib.amfls_gpu_policy_gradient.argtypes = [P, I, P, P, I, P, P, P]
     lib.amfls_gpu_policy_train.argtypes = [P, I, P, P, I, I, D, P, P, P]
+    lib.amfls_gpu_callback_operator_create.argtypes = [I, I, ctypes.POINTER(Callbacks), P,
+                                                       ctypes.POINTER(P)]
     lib.amfls_gpu_solve_amfls_batch.argtypes = [I, P, P, ctypes.POINTER(Options), P,
                                                 ctypes.POINTER(Result), P, I, P]
     lib.amfls_gpu_solve_amfls_controlled.argtypes = [P, P, ctypes.POINTER(Options), P, D, U64,

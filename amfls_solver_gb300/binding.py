@@ -202,6 +202,58 @@ class DeviceOperator:
         self.device = matrix.device
 
     @classmethod
+    def from_callbacks(cls, rows: int, cols: int, apply, apply_transpose, *,
+                       validation_model=None, relative_block_product_cost=None,
+                       device: torch.device | None = None) -> "DeviceOperator":
+        """A matrix-free operator (the reference's custom MatrixOperator).
+
+        apply(x, y) must write y = A x and apply_transpose(y, x) x = A^T y,
+        where x (cols, s) and y (rows, s) are float64 CUDA tensors viewing
+        the solver's column-major blocks; they run with torch's current
+        stream set to the solver's stream.  validation_model is
+        (norm_upper, norm_lower, apply_steps, transpose_steps) or None (then
+        no solve certifies success).  A callback that raises makes the solve
+        fail with an error."""
+        dev = device or torch.device("cuda", torch.cuda.current_device())
+
+        def view(ptr, nrows, s):
+            class _Block:  # column-major nrows x s float64 block at ptr
+                __cuda_array_interface__ = {"shape": (nrows, s), "typestr": "<f8",
+                                            "data": (ptr, False), "version": 2,
+                                            "strides": (8, 8 * nrows)}
+            return torch.as_tensor(_Block(), device=dev)
+
+        def wrap(fn, in_rows, out_rows):
+            def call(_ctx, src, s, dst, stream):
+                try:
+                    with torch.cuda.stream(torch.cuda.ExternalStream(stream or 0, device=dev)):
+                        fn(view(src, in_rows, s), view(dst, out_rows, s))
+                    return 0
+                except Exception:  # reported to the solver as a failed product
+                    return 1
+            return _native.APPLY_FN(call)
+
+        op = cls.__new__(cls)
+        op.rows, op.cols, op.device = int(rows), int(cols), dev
+        cb = _native.Callbacks()
+        cb.context = None
+        cb.apply = wrap(apply, op.cols, op.rows)
+        cb.apply_transpose = wrap(apply_transpose, op.rows, op.cols)
+        cb.relative_block_product_cost = (
+            _native.COST_FN(lambda _c, s: float(relative_block_product_cost(int(s))))
+            if relative_block_product_cost else _native.COST_FN())
+        if validation_model is not None:
+            cb.has_validation_model = 1
+            cb.validation_model = _native.ValidationModel(*validation_model)
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(dev):
+            _native.check(_native.load().amfls_gpu_callback_operator_create(
+                op.rows, op.cols, ctypes.byref(cb), _stream_handle(dev), ctypes.byref(handle)))
+        op.handle = handle
+        op._keep = cb  # the callbacks must outlive the operator
+        return op
+
+    @classmethod
     def from_csr_arrays(cls, rows, cols, row_offsets, column_indices, values):
         """CSR operator from device tensors (int64 offsets/indices, float64 values)."""
         t = torch.sparse_csr_tensor(row_offsets, column_indices, values, size=(rows, cols))
@@ -287,6 +339,29 @@ def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options: _na
 
 def _uint64(v: int) -> int:
     return int(v) & (2**64 - 1)
+
+
+def solve_amfls(op: DeviceOperator, b: torch.Tensor, *, regularization: float = 0.0,
+                tolerance: float = 1e-8, failure_probability: float = 1e-6,
+                maximum_epochs: int = 0, maximum_depth: int = 0,
+                maximum_auxiliary_width: int = 0, maximum_basis_size: int = 0, seed: int = 0,
+                stream: int = 0) -> SolveResult:
+    """AMFLS on an existing DeviceOperator (CSR, dense, reduced or callback),
+    the reference's C++ entry amfls::solve_amfls(op, b, options)
+    (include/amfls/amfls.hpp:22-25)."""
+    if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
+        raise ValueError("b must be a float64 CUDA vector of length rows on the operator's device")
+    o = _native.default_options()
+    o.regularization = float(regularization)
+    o.tolerance = float(tolerance)
+    o.failure_probability = float(failure_probability)
+    o.maximum_epochs = int(maximum_epochs)
+    o.maximum_depth = int(maximum_depth)
+    o.maximum_auxiliary_width = int(maximum_auxiliary_width)
+    o.maximum_basis_size = int(maximum_basis_size)
+    o.seed = _uint64(seed)
+    o.stream = _uint64(stream)
+    return _decode(_solve_raw("amfls", op, b, o))
 
 
 def run_amfls_batch(problems, *, workers: int = 16, regularization=0.0, tolerance=1e-8,

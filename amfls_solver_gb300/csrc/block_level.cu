@@ -66,7 +66,7 @@ void grow(T*& p, long long& cap, long long need, long long keep, cudaStream_t s)
 
 void Workspace::push_state() {
     AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
 }
 
 void Workspace::upload(double* dst, const std::vector<double>& src) {
@@ -74,7 +74,7 @@ void Workspace::upload(double* dst, const std::vector<double>& src) {
     AMFLS_CUDA(cudaMemcpyAsync(dst, src.data(), sizeof(double) * src.size(),
                                cudaMemcpyHostToDevice, stream_));
     // the host vector may die right after: make the copy complete
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
 }
 
 double Workspace::device_norm(const double* x, long long count) {
@@ -86,7 +86,7 @@ double Workspace::device_norm(const double* x, long long count) {
     norm_passes(set, dnorm_, partials_, counter_ + 1, stream_);
     NormResult h{};
     AMFLS_CUDA(cudaMemcpyAsync(&h, dnorm_, sizeof(NormResult), cudaMemcpyDeviceToHost, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     return euclid_from(h, 0);
 }
 
@@ -111,7 +111,7 @@ void Workspace::ensure_u_capacity(int cols) {
     stream_alloc(&u2, sizeof(double) * m_ * (size_t)cap, stream_);
     if (keep > 0)
         AMFLS_CUDA(cudaMemcpyAsync(u, U_, sizeof(double) * keep, cudaMemcpyDeviceToDevice, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     stream_free(U_, stream_);
     stream_free(U2_, stream_);
     U_ = u;
@@ -123,7 +123,7 @@ void Workspace::ensure_u_capacity(int cols) {
 void Workspace::ensure_block_capacity(int width) {
     if (width > bcap_) {
         const int cap = std::max(width, 2 * bcap_);
-        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        stream_wait(stream_);
         for (double** p : {&BR_, &BL_, &BQ_, &BT_}) {
             stream_free(*p, stream_);
             *p = nullptr;
@@ -160,7 +160,7 @@ void Workspace::enter_block_mode() {
         AMFLS_CUDA(cudaMemcpyAsync(be.data(), beta_, sizeof(double) * k, cudaMemcpyDeviceToHost, stream_));
         AMFLS_CUDA(cudaMemcpyAsync(g.data(), g_, sizeof(double) * host_.rows_t, cudaMemcpyDeviceToHost,
                                    stream_));
-        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        stream_wait(stream_);
         for (int j = 0; j < k; ++j) {
             const int nlw = be[j] != 0.0 ? 1 : 0;
             rec_meta_.insert(rec_meta_.end(), {1, 1, nlw, (int)rec_vals_.size(), (int)rec_state_size_});
@@ -233,7 +233,7 @@ Workspace::Factor Workspace::orthogonalize_and_factor(double* B, int cols, const
         if (retain)
             AMFLS_CUDA(cudaMemcpyAsync(h.data(), coefs_, sizeof(double) * h.size(),
                                        cudaMemcpyDeviceToHost, stream_));
-        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        stream_wait(stream_);
         coeff_finite = nf == 0;
         if (retain) {
             const size_t cnt = (size_t)kb * cols;
@@ -261,7 +261,7 @@ Workspace::Factor Workspace::orthogonalize_and_factor(double* B, int cols, const
             const double inv = 1.0 / resid;
             AMFLS_CUDA(cudaMemcpyAsync(sm, &inv, sizeof(double), cudaMemcpyHostToDevice, stream_));
             ts_nn(B, rows, sm, rows, 1, 1, q_out, rows, 1.0, 0.0, stream_);
-            AMFLS_CUDA(cudaStreamSynchronize(stream_));
+            stream_wait(stream_);
             F.rank = 1;
             F.factor = {resid};
         } else if (resid > 0.0 && resid <= F.cutoff) {
@@ -282,7 +282,7 @@ Workspace::Factor Workspace::orthogonalize_and_factor(double* B, int cols, const
     std::vector<double> hs(cols), hw(cc);
     AMFLS_CUDA(cudaMemcpyAsync(hs.data(), sig, sizeof(double) * cols, cudaMemcpyDeviceToHost, stream_));
     AMFLS_CUDA(cudaMemcpyAsync(hw.data(), W, sizeof(double) * cc, cudaMemcpyDeviceToHost, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     // a rows x cols block has min(rows, cols) singular values
     const int nsv = (int)std::min<long long>(rows, cols);
     int rank = 0;
@@ -311,7 +311,7 @@ Workspace::Factor Workspace::orthogonalize_and_factor(double* B, int cols, const
                                    stream_));
         AMFLS_CUDA(cudaMemcpyAsync(&chol_bad, dflags_ + 1, sizeof(int), cudaMemcpyDeviceToHost,
                                    stream_));
-        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        stream_wait(stream_);
         if (chol_bad) {
             // keep q = B W_r Sigma_r^{-1} as it is (U = I)
             AMFLS_CUDA(cudaMemcpyAsync(q_out, BT_, sizeof(double) * rows * rank,
@@ -338,7 +338,7 @@ Workspace::Factor Workspace::orthogonalize_and_factor(double* B, int cols, const
         for (int c = 0; c < tracked; ++c) weight = std::hypot(weight, hw[c + (size_t)idx * cols]);
         F.tracked = std::hypot(F.tracked, hs[idx] * weight);
     }
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     return F;
 }
 
@@ -488,7 +488,7 @@ bool Workspace::block_level() {
         ts_tn(U2_, m_, b_, m_, m_, nlw, 1, small_, bpart_, nullptr, stream_);
         AMFLS_CUDA(cudaMemcpyAsync(gnew.data(), small_, sizeof(double) * nlw, cudaMemcpyDeviceToHost,
                                    stream_));
-        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        stream_wait(stream_);
     }
     rec_meta_.insert(rec_meta_.end(), {r, aw, nlw, (int)rec_vals_.size(), (int)rec_state_size_});
     for (int c = 0; c < r; ++c)
@@ -552,7 +552,7 @@ const double* Workspace::block_projected_y(int* flags) {
                           stream_);
     rec_solved_ = levels;
     AMFLS_CUDA(cudaMemcpyAsync(flags, dflags_ + 2, sizeof(int), cudaMemcpyDeviceToHost, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     return d_y_;
 }
 

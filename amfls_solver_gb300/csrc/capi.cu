@@ -9,6 +9,7 @@
 
 #include "../../include/amfls_gpu.h"
 #include "batch.hpp"
+#include "callback_operator.hpp"
 #include "common.cuh"
 #include "controller.hpp"
 #include "csr_operator.hpp"
@@ -154,6 +155,29 @@ int amfls_gpu_dense_operator_create(int rows, int cols, const double* d_values, 
         auto h = std::make_unique<amfls_gpu_operator>();
         h->impl = std::make_unique<amfls_gpu::DenseOperator>(rows, cols, d_values,
                                                              column_major != 0, as_stream(stream));
+        *out = h.release();
+    });
+}
+
+int amfls_gpu_callback_operator_create(int rows, int cols,
+                                       const amfls_gpu_operator_callbacks* callbacks, void* stream,
+                                       amfls_gpu_operator** out) {
+    return guarded([&] {
+        if (out == nullptr) throw std::invalid_argument("output handle must not be null");
+        *out = nullptr;
+        if (callbacks == nullptr) throw std::invalid_argument("callbacks must not be null");
+        amfls_gpu::Callbacks cb;
+        cb.context = callbacks->context;
+        cb.apply = callbacks->apply;
+        cb.apply_transpose = callbacks->apply_transpose;
+        cb.relative_block_product_cost = callbacks->relative_block_product_cost;
+        cb.has_model = callbacks->has_validation_model != 0;
+        cb.model.norm_upper = callbacks->validation_model.operator_norm_upper_bound;
+        cb.model.norm_lower = callbacks->validation_model.operator_norm_lower_bound;
+        cb.model.apply_steps = callbacks->validation_model.apply_rounding_steps;
+        cb.model.transpose_steps = callbacks->validation_model.apply_transpose_rounding_steps;
+        auto h = std::make_unique<amfls_gpu_operator>();
+        h->impl = std::make_unique<amfls_gpu::CallbackOperator>(rows, cols, cb, as_stream(stream));
         *out = h.release();
     });
 }

@@ -54,6 +54,12 @@ inline void stream_free(const void* p, cudaStream_t s) {
 // buffers.  Called by each solve; takes effect once per device.
 void keep_pool_memory();
 
+// Waits until the work enqueued on `stream` so far has finished, blocking the
+// calling thread on a blocking-sync event instead of spinning (concurrent
+// solves on many host threads then leave the CPU cores to the threads that
+// launch work).
+void stream_wait(cudaStream_t stream);
+
 constexpr int kWarp = 32;
 constexpr int kPanel = 32;  // columns per V panel (row-major n x 32 tiles)
 

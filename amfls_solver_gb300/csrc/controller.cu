@@ -584,7 +584,8 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
     const auto t_start = Clock::now();
     const long long launches0 = launch_count();
     Statistics stats;
-    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators, o.use_graphs);
+    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators,
+                 o.use_graphs && op.graph_safe());
     Evaluator ev(ws, op, d_b, reg, stats, stream);
     long long seen[4] = {0, 0, 0, 0};
     auto absorb = [&] {
@@ -655,7 +656,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
         out.stop_reason = reason;
         AMFLS_CUDA(cudaMemcpyAsync(d_solution, ev.buffer(c.buffer), sizeof(double) * op.cols(),
                                    cudaMemcpyDeviceToDevice, stream));
-        AMFLS_CUDA(cudaStreamSynchronize(stream));
+        stream_wait(stream);
         stats.total_seconds = seconds_since(t_start);
         stats.kernel_launches = launch_count() - launches0;
         out.statistics = stats;
@@ -684,8 +685,8 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
     bool feedback = false;
     int fb_target = 0, stage_rank = 0, stage_origin = 0, stage_target = 0;
     cudaEvent_t iv0, iv1;
-    AMFLS_CUDA(cudaEventCreate(&iv0));
-    AMFLS_CUDA(cudaEventCreate(&iv1));
+    AMFLS_CUDA(cudaEventCreateWithFlags(&iv0, cudaEventBlockingSync));
+    AMFLS_CUDA(cudaEventCreateWithFlags(&iv1, cudaEventBlockingSync));
     struct EventGuard {
         cudaEvent_t a, b;
         ~EventGuard() {
@@ -909,7 +910,8 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
     const auto t_start = Clock::now();
     const long long launches0 = launch_count();
     Statistics stats;
-    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators, o.use_graphs);
+    Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators,
+                 o.use_graphs && op.graph_safe());
     Evaluator ev(ws, op, d_b, reg, stats, stream);
     long long seen[4] = {0, 0, 0, 0};
     auto absorb = [&] {
@@ -1045,7 +1047,7 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
     out.stop_reason = reason;
     AMFLS_CUDA(cudaMemcpyAsync(d_solution, ev.buffer(result.buffer), sizeof(double) * op.cols(),
                                cudaMemcpyDeviceToDevice, stream));
-    AMFLS_CUDA(cudaStreamSynchronize(stream));
+    stream_wait(stream);
     stats.total_seconds = seconds_since(t_start);
     stats.kernel_launches = launch_count() - launches0;
     out.statistics = stats;

@@ -104,8 +104,12 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char* wbase = smem + warp * warp_smem_bytes<C, E>();
     using A = acc_t<V>;
-    A* vs = reinterpret_cast<A*>(wbase);           // E values
-    A* xs = reinterpret_cast<A*>(wbase + E * 8);   // E x C gathered x
+    A* vs = reinterpret_cast<A*>(wbase);           // E values (C > 1)
+    A* xs = reinterpret_cast<A*>(wbase + E * 8);   // E x C gathered x (C > 1)
+    // one column: (value, x) pairs, one 16-byte (8-byte for FP32) word each,
+    // so the row sums read both with one shared-memory access
+    using Pair = std::conditional_t<std::is_same_v<A, double>, double2, float2>;
+    Pair* vx = reinterpret_cast<Pair*>(wbase);
     int* ro = reinterpret_cast<int*>(wbase + E * 8 + E * C * 8);  // E + 1 row offsets
     constexpr int kPer = E / 32;
 
@@ -199,8 +203,10 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
             for (int u = 0; u < kPer; ++u) xv[u] = j[u] >= 0 ? to_acc<A>(__ldg(x + j[u])) : A(0);
 #pragma unroll
             for (int u = 0; u < kPer; ++u) {
-                vs[lane + 32 * u] = a[u];
-                xs[lane + 32 * u] = xv[u];
+                Pair p;
+                p.x = a[u];
+                p.y = xv[u];
+                vx[lane + 32 * u] = p;
             }
         } else {
             static_assert(C % 2 == 0, "multi-column tiles gather pairs of doubles");
@@ -242,27 +248,19 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                     wide |= 1u << k;
                     continue;
                 }
-                A acc[C];
-#pragma unroll
-                for (int c = 0; c < C; ++c) acc[c] = 0;
+                A acc[C];  // C == 1 on this path
+                acc[0] = 0;
                 int e = b0;
                 for (; e + 4 <= b1; e += 4) {
-                    A av[4], xv[4][C];
+                    Pair p[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        av[u] = vs[e + u];
+                    for (int u = 0; u < 4; ++u) p[u] = vx[e + u];
 #pragma unroll
-                        for (int c = 0; c < C; ++c) xv[u][c] = xs[(e + u) * C + c];
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int c = 0; c < C; ++c) acc[c] = fma(av[u], xv[u][c], acc[c]);
+                    for (int u = 0; u < 4; ++u) acc[0] = fma(p[u].x, p[u].y, acc[0]);
                 }
                 for (; e < b1; ++e) {
-                    const A av = vs[e];
-#pragma unroll
-                    for (int c = 0; c < C; ++c) acc[c] = fma(av, xs[e * C + c], acc[c]);
+                    const Pair p = vx[e];
+                    acc[0] = fma(p.x, p.y, acc[0]);
                 }
                 const int r = d.x + i;
                 if constexpr (kFused) {
@@ -291,7 +289,10 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
                 const int i = mine ? wl[w0 + g] : 0;
                 const int b0 = mine ? ro[i] : 0, b1 = mine ? ro[i + 1] : 0;
                 A acc = 0;
-                for (int e = b0 + gl; e < b1; e += 8) acc = fma(vs[e], xs[e], acc);
+                for (int e = b0 + gl; e < b1; e += 8) {
+                    const Pair p = vx[e];
+                    acc = fma(p.x, p.y, acc);
+                }
 #pragma unroll
                 for (int o = 4; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                 if (mine && gl == 0) {

@@ -121,8 +121,13 @@ public:
         return false;
     }
     // Storage kind for diagnostics: 0 CSR, 1 row-major dense, 2 column-major
-    // dense, 3 custom callbacks.
+    // dense, 3 custom callbacks or a composition.
     virtual int kind() const = 0;
+    // Whether the products only enqueue device work on the stream they are
+    // given (no host synchronisation, no allocation), so that they may be
+    // captured into a CUDA graph.  The built-in operators are; operators
+    // that call user code are not assumed to be.
+    virtual bool graph_safe() const { return true; }
 };
 
 }  // namespace amfls_gpu

@@ -207,7 +207,7 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
             AMFLS_LAUNCHED();
         }
     }
-    AMFLS_CUDA(cudaStreamSynchronize(stream));
+    stream_wait(stream);
     out.statistics.total_seconds =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     out.statistics.kernel_launches = launch_count() - launches0;

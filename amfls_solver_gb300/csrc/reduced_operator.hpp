@@ -65,6 +65,7 @@ public:
     int rows() const override { return a_.rows() + a_.cols(); }
     int cols() const override { return a_.cols(); }
     int kind() const override { return 3; }
+    bool graph_safe() const override { return a_.graph_safe(); }
     void apply(const double* x, int block_cols, double* y, cudaStream_t s) const override;
     void apply_transpose(const double* y, int block_cols, double* x,
                          cudaStream_t s) const override;

@@ -620,8 +620,8 @@ struct Validator::Impl {
         alloc(partials, 2 * kMaxVectors * 1216 + 8 * 1216);
         stream_alloc(&counters, sizeof(unsigned) * 16, stream);
         AMFLS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned) * 16, stream));
-        AMFLS_CUDA(cudaEventCreate(&ev[0]));
-        AMFLS_CUDA(cudaEventCreate(&ev[1]));
+        AMFLS_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventBlockingSync));
+        AMFLS_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventBlockingSync));
     }
     ~Impl() {
         cudaStreamSynchronize(stream);
@@ -679,7 +679,7 @@ struct Validator::Impl {
     ValState read() {
         ValState h;
         AMFLS_CUDA(cudaMemcpyAsync(&h, vs, sizeof(ValState), cudaMemcpyDeviceToHost, stream));
-        AMFLS_CUDA(cudaStreamSynchronize(stream));
+        stream_wait(stream);
         return h;
     }
 

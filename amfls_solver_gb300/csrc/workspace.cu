@@ -47,6 +47,27 @@ void keep_pool_memory() {
     done[dev] = true;
 }
 
+void stream_wait(cudaStream_t stream) {
+    struct Event {
+        cudaEvent_t e = nullptr;
+        int device = -1;
+        ~Event() {
+            if (e) cudaEventDestroy(e);
+        }
+    };
+    thread_local Event ev;
+    int dev = 0;
+    AMFLS_CUDA(cudaGetDevice(&dev));
+    if (!ev.e || ev.device != dev) {
+        if (ev.e) cudaEventDestroy(ev.e);
+        ev.e = nullptr;
+        AMFLS_CUDA(cudaEventCreateWithFlags(&ev.e, cudaEventBlockingSync | cudaEventDisableTiming));
+        ev.device = dev;
+    }
+    AMFLS_CUDA(cudaEventRecord(ev.e, stream));
+    AMFLS_CUDA(cudaEventSynchronize(ev.e));
+}
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -639,7 +660,7 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     host_.reliable = 1;
     host_.basis_limit = basis_limit_;
     AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
 }
 
 Workspace::~Workspace() {
@@ -688,7 +709,7 @@ void Workspace::ensure_t_capacity(int cols) {
     if (cols + 2 <= tcap_ && cols <= ccap_) return;
     int cap = std::max(1024, tcap_);
     while (cap < cols + 2) cap *= 2;
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     auto grow = [&](double*& p, size_t old_count, size_t new_count) {
         double* q = nullptr;
         stream_alloc(&q, sizeof(double) * new_count, stream_);
@@ -696,7 +717,7 @@ void Workspace::ensure_t_capacity(int cols) {
         if (p) {
             AMFLS_CUDA(cudaMemcpyAsync(q, p, sizeof(double) * old_count, cudaMemcpyDeviceToDevice,
                                        stream_));
-            AMFLS_CUDA(cudaStreamSynchronize(stream_));
+            stream_wait(stream_);
             stream_free(p, stream_);
         }
         p = q;
@@ -720,7 +741,7 @@ void Workspace::ensure_t_capacity(int cols) {
 
 void Workspace::invalidate_graph() {
     if (graph_exec_) {
-        AMFLS_CUDA(cudaStreamSynchronize(stream_));
+        stream_wait(stream_);
         cudaGraphExecDestroy(graph_exec_);
         graph_exec_ = nullptr;
     }
@@ -744,7 +765,7 @@ void Workspace::initialize(const double* d_aux, int aux_cols) {
     norm_passes(set, nr, partials_, counter_ + 1, stream_);
     NormResult h{};
     AMFLS_CUDA(cudaMemcpyAsync(&h, nr, sizeof(NormResult), cudaMemcpyDeviceToHost, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     AMFLS_CUDA(cudaFreeAsync(nr, stream_));
     if (h.nonfinite[0]) throw std::invalid_argument("block Golub-Kahan right-hand side must be finite");
     b_norm_ = euclid_from(h, 0);
@@ -761,7 +782,7 @@ void Workspace::initialize(const double* d_aux, int aux_cols) {
     }
     std::memset(&host_.audit, 0, sizeof(host_.audit));
     AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     if (b_norm_ > 0.0 && aux_cols > 0) append_left_seed(d_aux, aux_cols);
 }
 
@@ -902,7 +923,7 @@ bool Workspace::advance_level() {
 
 void Workspace::sync() {
     AMFLS_CUDA(cudaMemcpyAsync(&host_, dstate_, sizeof(DevState), cudaMemcpyDeviceToHost, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     if (use_graphs_) {  // kernels the device ran inside graph-launched intervals
         launch_count() += body_kernels_ * (host_.body_runs - counted_body_runs_);
     }
@@ -944,7 +965,7 @@ void Workspace::solve_projected(double* d_x) {
     AMFLS_LAUNCHED();
     double st[8];
     AMFLS_CUDA(cudaMemcpyAsync(st, qr_state_, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream_));
-    AMFLS_CUDA(cudaStreamSynchronize(stream_));
+    stream_wait(stream_);
     projected_flags_ = (int)st[5];
 }
 

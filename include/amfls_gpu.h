@@ -112,6 +112,30 @@ int amfls_gpu_csr_operator_create(int rows, int cols, const int64_t* d_row_offse
 int amfls_gpu_dense_operator_create(int rows, int cols, const double* d_values, int column_major,
                                     void* stream, amfls_gpu_operator** out);
 
+/* A matrix-free operator over caller callbacks, the C-ABI form of the
+ * reference's custom MatrixOperator subclasses (matrix_operator.hpp:29-89).
+ * apply computes Y (rows x s) = A X (cols x s), apply_transpose X = A^T Y,
+ * on column-major device blocks, enqueuing their work on `stream` (the
+ * result must be ready in stream order); they return 0 on success.
+ * relative_block_product_cost may be NULL (the interface default s).
+ * Without a validation model (has_validation_model = 0) no solve certifies
+ * success, as in the reference (matrix_operator.hpp:17-20).  The solver
+ * calls the callbacks from the calling thread and never inside a CUDA graph
+ * capture.  The context and callbacks must outlive the operator. */
+typedef struct {
+    void* context;
+    int (*apply)(void* context, const double* d_x, int block_cols, double* d_y, void* stream);
+    int (*apply_transpose)(void* context, const double* d_y, int block_cols, double* d_x,
+                           void* stream);
+    double (*relative_block_product_cost)(void* context, int block_cols);
+    int has_validation_model;
+    amfls_gpu_validation_error_model validation_model;
+} amfls_gpu_operator_callbacks;
+
+int amfls_gpu_callback_operator_create(int rows, int cols,
+                                       const amfls_gpu_operator_callbacks* callbacks, void* stream,
+                                       amfls_gpu_operator** out);
+
 int amfls_gpu_operator_destroy(amfls_gpu_operator* op);
 int amfls_gpu_operator_rows(const amfls_gpu_operator* op);
 int amfls_gpu_operator_cols(const amfls_gpu_operator* op);

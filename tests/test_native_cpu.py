@@ -83,3 +83,12 @@ def test_mixed_entry_points_reject_bad_arguments(lib):
     rc = lib.amfls_gpu_solve_amfls_mixed(None, None, None, ctypes.byref(o), 1e-6, 4, None,
                                          ctypes.byref(res), None, None, 0, None)
     assert rc == 1 and b"operator must not be null" in lib.amfls_gpu_last_error()
+
+
+def test_callback_operator_needs_both_products(lib):
+    cb = _native.Callbacks()
+    handle = ctypes.c_void_p()
+    rc = lib.amfls_gpu_callback_operator_create(10, 5, ctypes.byref(cb), None, ctypes.byref(handle))
+    assert rc == 1 and b"apply and apply_transpose" in lib.amfls_gpu_last_error()
+    rc = lib.amfls_gpu_callback_operator_create(10, 5, None, None, ctypes.byref(handle))
+    assert rc == 1 and handle.value is None
