@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdint>
 #include <memory>
+#include <numeric>
 #include <stdexcept>
 #include <type_traits>
 #include <utility>
@@ -242,25 +243,31 @@ long long padded(long long n) { return ((n + 3) & ~3LL) + 4; }
 struct TileStore {
     int4* tiles = nullptr;
     int* split = nullptr;
+    int2* chain = nullptr;
     int2* long_rows = nullptr;
     unsigned* long_count = nullptr;
     double* long_part = nullptr;
     int ntiles = 0;
+    int nnz = 0;
+    bool chains = false;  // chain groups rather than row blocks
     int grid = 1;
 
     csr_tiles::Table view() const {
         csr_tiles::Table t;
         t.tiles = tiles;
         t.split = split;
+        t.chain = chain;
         t.long_rows = long_rows;
         t.long_count = long_count;
         t.long_part = long_part;
         t.ntiles = ntiles;
+        t.nnz = nnz;
         return t;
     }
     void release() {
         cudaFree(tiles);
         cudaFree(split);
+        cudaFree(chain);
         cudaFree(long_rows);
         cudaFree(long_count);
         cudaFree(long_part);
@@ -268,44 +275,142 @@ struct TileStore {
     }
 };
 
-// Greedy cut of rows [0, count) with host offsets `off` into row blocks of at
-// most E nonzeros and E rows, single rows of up to kRowTaskTiles E nonzeros,
-// and kRowTaskTiles E-element slices of longer rows (see csr_tiles.cuh).
-void make_tiles(const std::vector<long long>& off, int count, int E, int C, TileStore& ts,
-                cudaStream_t stream) {
+// Warp tasks of one side: rows longer than `longer_than` as whole-row
+// tasks (up to kRowTaskTiles E nonzeros) or kRowTaskTiles E-element slices;
+// the other rows either as chain groups or as greedy row blocks of at most
+// E nonzeros and E rows (see csr_tiles.cuh).  Chain groups are used for
+// single-column tables (chains == true) of sides whose median row has at
+// most kChainShort nonzeros: there row blocks leave most lanes of every FMA
+// idle behind the block's longest row, while on sides of longer rows a
+// chain group needs many dependent staging passes and row blocks (a few
+// rows of 8-lane sums) finish sooner.  The table lists tasks by estimated
+// latency, longest first (stable, so that the groups of a window stay
+// together), for the kernel's snake-order assignment of tasks to warps.
+void make_tiles(const std::vector<long long>& off, int count, int E, int C, bool chains,
+                TileStore& ts, cudaStream_t stream) {
+    using namespace csr_tiles;
     std::vector<int4> tiles;
     std::vector<int> split;
-    std::vector<int2> long_rows;
-    int r = 0;
-    while (r < count) {
-        const long long len = off[r + 1] - off[r];
-        const long long task = (long long)csr_tiles::kRowTaskTiles * E;
+    std::vector<int2> chain, long_rows;
+    std::vector<int> cost;  // dependent memory round trips of the task
+    auto length = [&](int r) { return off[r + 1] - off[r]; };
+    if (chains && count > 0) {
+        std::vector<long long> lens(count);
+        for (int r = 0; r < count; ++r) lens[r] = length(r);
+        std::nth_element(lens.begin(), lens.begin() + count / 2, lens.end());
+        chains = lens[count / 2] <= kChainShort;
+    }
+    const long long longer_than = chains ? kChainMax : E;
+    const long long task = (long long)kRowTaskTiles * E;
+    for (int r = 0; r < count; ++r) {
+        const long long len = length(r);
+        if (len <= longer_than) continue;
         if (len > task) {  // slices of one warp task each
             const int first = (int)tiles.size();
             for (long long e = off[r]; e < off[r + 1]; e += task) {
                 tiles.push_back(make_int4(r, r + 1, (int)e, (int)std::min(e + task, off[r + 1])));
                 split.push_back((int)long_rows.size());
+                cost.push_back(2 * kRowTaskTiles + 2);
             }
             long_rows.push_back(make_int2(first, (int)tiles.size() - first));
-            ++r;
-            continue;
-        }
-        if (len > E) {  // one warp task for the whole row
+        } else {  // one warp task for the whole row
             tiles.push_back(make_int4(r, r + 1, (int)off[r], (int)off[r + 1]));
-            split.push_back(-2);
-            ++r;
-            continue;
+            split.push_back(kWholeRow);
+            cost.push_back(2 * (int)((len + E - 1) / E) + 1);
         }
-        const int r0 = r;
-        const long long e0 = off[r];
-        while (r < count && off[r + 1] - e0 <= E && r - r0 < E) ++r;
-        tiles.push_back(make_int4(r0, r, (int)e0, (int)off[r]));
-        split.push_back(-1);
     }
+    // groups of consecutive entries of `rows` (sorted by length): up to
+    // kFlatRows rows while none is longer than one, else up to 32
+    auto add_groups = [&](const std::vector<int>& rows) {
+        size_t g = 0;
+        while (g < rows.size()) {
+            long long longest = 0;
+            size_t end = g;
+            while (end < rows.size()) {
+                const long long l = std::max(longest, length(rows[end]));
+                if (end - g + 1 > (l <= 1 ? (size_t)kFlatRows : (size_t)32)) break;
+                longest = l;
+                ++end;
+            }
+            tiles.push_back(make_int4((int)chain.size(), (int)(end - g), (int)longest, 0));
+            split.push_back(kChainGroup);
+            cost.push_back(2 * (int)((longest + kChainStep - 1) / kChainStep) + 2);
+            for (size_t i = g; i < end; ++i)
+                chain.push_back(make_int2(rows[i], length(rows[i]) > 0 ? (int)off[rows[i]] : -1));
+            g = end;
+        }
+    };
+    if (chains) {
+        // chain rows longer than kChainShort: by length (longest first) over
+        // the whole side, stable in row order
+        std::vector<int> rows;
+        for (int r = 0; r < count; ++r)
+            if (length(r) > kChainShort && length(r) <= kChainMax) rows.push_back(r);
+        std::stable_sort(rows.begin(), rows.end(),
+                         [&](int a, int b) { return length(a) > length(b); });
+        add_groups(rows);
+        // short rows: windows of kChainWindow consecutive ones, sorted by
+        // length within the window (a counting sort, stable in row order)
+        std::vector<int> window, sorted;
+        auto flush = [&] {
+            std::vector<int> start(kChainShort + 2, 0);
+            for (int r : window) ++start[length(r) + 1];
+            for (int l = 0; l <= kChainShort; ++l) start[l + 1] += start[l];
+            sorted.assign(window.size(), 0);
+            for (int r : window) sorted[start[length(r)]++] = r;
+            add_groups(sorted);
+            window.clear();
+        };
+        for (int r = 0; r < count; ++r) {
+            if (length(r) > kChainShort) continue;
+            window.push_back(r);
+            if ((int)window.size() == kChainWindow) flush();
+        }
+        if (!window.empty()) flush();
+    } else {
+        int r = 0;
+        while (r < count) {
+            if (length(r) > longer_than) {
+                ++r;
+                continue;
+            }
+            const int r0 = r;
+            const long long e0 = off[r];
+            while (r < count && length(r) <= longer_than && off[r + 1] - e0 <= E && r - r0 < E)
+                ++r;
+            tiles.push_back(make_int4(r0, r, (int)e0, (int)off[r]));
+            split.push_back(kRowBlock);
+            cost.push_back(3);
+        }
+    }
+    // longest first; slices of one row stay adjacent (equal cost, inserted
+    // together), and each long row's first slice index follows the move
+    std::vector<int> order(tiles.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<int4> tiles_sorted(tiles.size());
+    std::vector<int> split_sorted(tiles.size());
+    std::vector<char> seen(long_rows.size(), 0);
+    for (size_t i = 0; i < order.size(); ++i) {
+        tiles_sorted[i] = tiles[order[i]];
+        split_sorted[i] = split[order[i]];
+        const int q = split_sorted[i];
+        if (q >= 0 && !seen[q]) {
+            seen[q] = 1;
+            long_rows[q].x = (int)i;
+        }
+    }
+    tiles.swap(tiles_sorted);
+    split.swap(split_sorted);
+
     ts.ntiles = (int)tiles.size();
+    ts.nnz = (int)off[count];
+    ts.chains = chains;
     const size_t nt = std::max<size_t>(1, tiles.size()), nl = std::max<size_t>(1, long_rows.size());
+    const size_t nc = std::max<size_t>(1, chain.size());
     AMFLS_CUDA(cudaMalloc(&ts.tiles, sizeof(int4) * nt));
     AMFLS_CUDA(cudaMalloc(&ts.split, sizeof(int) * nt));
+    AMFLS_CUDA(cudaMalloc(&ts.chain, sizeof(int2) * nc));
     AMFLS_CUDA(cudaMalloc(&ts.long_rows, sizeof(int2) * nl));
     AMFLS_CUDA(cudaMalloc(&ts.long_count, sizeof(unsigned) * nl));
     AMFLS_CUDA(cudaMalloc(&ts.long_part, sizeof(double) * C * nt));
@@ -316,6 +421,9 @@ void make_tiles(const std::vector<long long>& off, int count, int E, int C, Tile
         AMFLS_CUDA(cudaMemcpyAsync(ts.split, split.data(), sizeof(int) * split.size(),
                                    cudaMemcpyHostToDevice, stream));
     }
+    if (!chain.empty())
+        AMFLS_CUDA(cudaMemcpyAsync(ts.chain, chain.data(), sizeof(int2) * chain.size(),
+                                   cudaMemcpyHostToDevice, stream));
     if (!long_rows.empty())
         AMFLS_CUDA(cudaMemcpyAsync(ts.long_rows, long_rows.data(),
                                    sizeof(int2) * long_rows.size(), cudaMemcpyHostToDevice,
@@ -341,35 +449,50 @@ __global__ void rows_major_kernel(const double* __restrict__ x, long long ld, in
 
 // Resident CTAs for a tile kernel (every warp of the grid walks its own
 // tiles), at most one warp per tile and at most kMaxBlocks CTAs.
-template <typename V, int C, int E, bool kFused>
+template <typename V, int C, int E, bool kFused, bool kChains>
 int tile_grid(int ntiles) {
     // resident CTAs per SM and SM count, set up once per instantiation (a
     // function-local static is initialised once even with concurrent callers)
     static const std::pair<int, int> occ = [] {
         constexpr int bytes = csr_tiles::smem_bytes<C, E>();
-        AMFLS_CUDA(cudaFuncSetAttribute(csr_tiles::tile_product_kernel<V, C, E, kFused>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        auto kernel = csr_tiles::tile_product_kernel<V, C, E, kFused, kChains>;
+        AMFLS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         int dev = 0, nb = 0, sms = 0;
         AMFLS_CUDA(cudaGetDevice(&dev));
         AMFLS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, csr_tiles::tile_product_kernel<V, C, E, kFused>, csr_tiles::kThreads, bytes));
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, csr_tiles::kThreads,
+                                                                 bytes));
         return std::make_pair(std::max(1, nb), sms);
     }();
     const int need = (ntiles + csr_tiles::kWarps - 1) / csr_tiles::kWarps;
     return std::max(1, std::min({need, occ.first * occ.second, kMaxBlocks}));
 }
 
+template <int C, bool kFused, bool kChains, typename V>
+void launch_tiles_as(const int* off, const int* idx, const V* val, const TileStore& ts,
+                     const double* x, double* y, long long ldy, int ncols, const Epilogue& ep,
+                     double* partials, unsigned* counter, cudaStream_t stream) {
+    constexpr int E = C == 1 ? csr_tiles::kE1 : csr_tiles::kEC;
+    const int grid = tile_grid<V, C, E, kFused, kChains>(ts.ntiles);
+    csr_tiles::tile_product_kernel<V, C, E, kFused, kChains>
+        <<<grid, csr_tiles::kThreads, csr_tiles::smem_bytes<C, E>(), stream>>>(
+            off, idx, val, ts.view(), x, y, ldy, ncols, ep, partials, counter);
+    AMFLS_LAUNCHED();
+}
+
 template <int C, bool kFused, typename V>
 void launch_tiles(const int* off, const int* idx, const V* val, const TileStore& ts,
                   const double* x, double* y, long long ldy, int ncols, const Epilogue& ep,
                   double* partials, unsigned* counter, cudaStream_t stream) {
-    constexpr int E = C == 1 ? csr_tiles::kE1 : csr_tiles::kEC;
-    const int grid = tile_grid<V, C, E, kFused>(ts.ntiles);
-    csr_tiles::tile_product_kernel<V, C, E, kFused>
-        <<<grid, csr_tiles::kThreads, csr_tiles::smem_bytes<C, E>(), stream>>>(
-            off, idx, val, ts.view(), x, y, ldy, ncols, ep, partials, counter);
-    AMFLS_LAUNCHED();
+    if constexpr (C == 1) {
+        if (ts.chains) {
+            launch_tiles_as<C, kFused, true>(off, idx, val, ts, x, y, ldy, ncols, ep, partials,
+                                             counter, stream);
+            return;
+        }
+    }
+    launch_tiles_as<C, kFused, false>(off, idx, val, ts, x, y, ldy, ncols, ep, partials, counter,
+                                      stream);
 }
 
 }  // namespace
@@ -382,8 +505,8 @@ struct CsrOperator::Side {
     int* perm = nullptr;       // count (rows sorted by bin, double-double products)
     BinTable bins{};
     int count = 0;
-    TileStore one;             // tiles of kE1 elements: single-column products
-    TileStore many;            // tiles of kEC elements: 2..8 columns
+    TileStore one;             // single-column products: chain groups or row blocks, long rows
+    TileStore many;            // row blocks of kEC elements: 2..8 columns
 };
 
 CsrOperator::CsrOperator(int rows, int cols, const long long* d_offsets,
@@ -609,8 +732,8 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
         AMFLS_CUDA(cudaMemcpyAsync(host_off.data(), sd->off, sizeof(long long) * (sd->count + 1),
                                    cudaMemcpyDeviceToHost, stream));
         AMFLS_CUDA(cudaStreamSynchronize(stream));
-        make_tiles(host_off, sd->count, csr_tiles::kE1, 1, sd->one, stream);
-        make_tiles(host_off, sd->count, csr_tiles::kEC, 8, sd->many, stream);
+        make_tiles(host_off, sd->count, csr_tiles::kE1, 1, true, sd->one, stream);
+        make_tiles(host_off, sd->count, csr_tiles::kEC, 8, false, sd->many, stream);
     }
 
     // certified norm model

@@ -22,9 +22,16 @@ __device__ __forceinline__ void epilogue_row(const Epilogue& ep, int row, double
         sq_t = fma(t, t, sq_t);
         sq_out = fma(out, out, sq_out);
         if (ep.dot_vec) dot = fma(out, ep.dot_vec[row], dot);
-        mx_t = fmax(mx_t, fabs(t));
-        mx_out = fmax(mx_out, fabs(out));
-        if (!isfinite(t) || !isfinite(out)) ++nonfin;
+        // fmax(mx, |v|) (NaN ignored) and the finiteness test on the bit
+        // patterns, off the FP64 pipe: magnitudes of non-NaN doubles order
+        // like their bits, and mx starts at +0 so it is never NaN
+        constexpr unsigned long long kInf = 0x7ff0000000000000ull;
+        const unsigned long long at = __double_as_longlong(t) & 0x7fffffffffffffffull;
+        const unsigned long long ao = __double_as_longlong(out) & 0x7fffffffffffffffull;
+        const unsigned long long mt = __double_as_longlong(mx_t), mo = __double_as_longlong(mx_out);
+        if (at <= kInf && at > mt) mx_t = __longlong_as_double(at);
+        if (ao <= kInf && ao > mo) mx_out = __longlong_as_double(ao);
+        if (at >= kInf || ao >= kInf) ++nonfin;
     }
 }
 

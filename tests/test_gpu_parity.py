@@ -149,6 +149,48 @@ def test_csr_tiled_products_long_and_empty_rows(amfls):
     assert np.all(ax[lens == 0] == 0.0)
 
 
+def chain_csr(seed=11, m=5000, n=700):
+    """Every row length from 0 to 300 (most rows short) in shuffled order, so
+    single-column products see chain groups from windows of short rows, chain
+    groups of rows sorted by length up to 64, and whole long rows; columns
+    hold about 100-170 entries each (whole rows on the transpose side)."""
+    from amfls_solver_gb300 import problems
+
+    rng = np.random.default_rng(seed)
+    lens = np.concatenate([np.arange(301), rng.integers(0, 5, 3500),
+                           rng.integers(5, 65, m - 301 - 3500)])
+    rng.shuffle(lens)
+    rows = [np.sort(rng.choice(n, int(ln), replace=False)) for ln in lens]
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    col = np.concatenate(rows).astype(np.int64)
+    val = rng.standard_normal(col.size)
+    return problems.CsrProblem(m, n, off, col, val, np.zeros(m))
+
+
+def test_csr_single_column_chains_bit_exact(amfls):
+    """Single-column products sum every row (and column) of up to 64
+    nonzeros as one FMA chain in storage order from 0, as the reference's
+    SparseCsrOperator::apply / apply_transpose do, so those entries are
+    bit-identical to the oracle's; longer ones are within gamma_{2L+2}."""
+    prob = chain_csr()
+    op = amfls.DeviceOperator(csr_tensor(prob))
+    ref = orc.Operator(prob)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((prob.cols, 1))
+    y = rng.standard_normal((prob.rows, 1))
+    ax = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()[:, 0]
+    aty = op.apply(torch.from_numpy(y).cuda(), transpose=True).cpu().numpy()[:, 0]
+    ax_ref = ref.apply(np.asfortranarray(x))[:, 0]
+    aty_ref = ref.apply_transpose(np.asfortranarray(y))[:, 0]
+    lens = np.diff(prob.row_offsets)
+    clens = np.bincount(prob.column_indices, minlength=prob.cols)
+    assert (lens > 64).any() and (lens <= 64).sum() > 4000
+    assert np.array_equal(ax[lens <= 64], ax_ref[lens <= 64])
+    assert np.array_equal(aty[clens <= 64], aty_ref[clens <= 64])
+    assert np.all(np.abs(ax - ax_ref) <= 2 * product_bound(prob, x[:, 0], False))
+    assert np.all(np.abs(aty - aty_ref) <= 2 * product_bound(prob, y[:, 0], True))
+
+
 @pytest.mark.parametrize("name", ["dense_model_rm", "dense_model_cm"])
 def test_dense_model_matches_reference(amfls, name):
     data, prob = load_golden(name)
