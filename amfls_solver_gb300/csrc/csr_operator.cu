@@ -25,9 +25,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <memory>
 #include <numeric>
 #include <stdexcept>
+#include <string>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -275,17 +277,26 @@ struct TileStore {
     }
 };
 
+// Sides with fewer nonzeros use row blocks even when their rows are short:
+// their tables hold about one task per resident warp, so a product takes
+// as long as its slowest task, and a chain group (several dependent staging
+// passes) is slower than a row block (one load round, one gather round).
+constexpr long long kChainMinNonzeros = 1LL << 21;
+
 // Warp tasks of one side: rows longer than `longer_than` as whole-row
 // tasks (up to kRowTaskTiles E nonzeros) or kRowTaskTiles E-element slices;
 // the other rows either as chain groups or as greedy row blocks of at most
 // E nonzeros and E rows (see csr_tiles.cuh).  Chain groups are used for
-// single-column tables (chains == true) of sides whose median row has at
-// most kChainShort nonzeros: there row blocks leave most lanes of every FMA
-// idle behind the block's longest row, while on sides of longer rows a
-// chain group needs many dependent staging passes and row blocks (a few
-// rows of 8-lane sums) finish sooner.  The table lists tasks by estimated
-// latency, longest first (stable, so that the groups of a window stay
-// together), for the kernel's snake-order assignment of tasks to warps.
+// single-column tables (chains == true) of sides with at least
+// kChainMinNonzeros nonzeros whose median row has at most kChainShort:
+// there row blocks leave most lanes of every FMA idle behind the block's
+// longest row, while on sides of longer rows a chain group needs many
+// dependent staging passes and row blocks (a few rows of 8-lane sums)
+// finish sooner.  AMFLS_GB300_CSR_CHAINS=0 in the environment turns chain
+// groups off, =1 drops the size condition (for tests on small matrices).
+// The table lists tasks by estimated latency, longest first (stable, so
+// that the groups of a window stay together), for the kernel's snake-order
+// assignment of tasks to warps.
 void make_tiles(const std::vector<long long>& off, int count, int E, int C, bool chains,
                 TileStore& ts, cudaStream_t stream) {
     using namespace csr_tiles;
@@ -294,7 +305,13 @@ void make_tiles(const std::vector<long long>& off, int count, int E, int C, bool
     std::vector<int2> chain, long_rows;
     std::vector<int> cost;  // dependent memory round trips of the task
     auto length = [&](int r) { return off[r + 1] - off[r]; };
-    if (chains && count > 0) {
+    if (chains) {
+        const char* mode = std::getenv("AMFLS_GB300_CSR_CHAINS");
+        const bool off_mode = mode && std::string(mode) == "0";
+        const bool any_size = mode && std::string(mode) == "1";
+        chains = !off_mode && count > 0 && (any_size || off[count] >= kChainMinNonzeros);
+    }
+    if (chains) {
         std::vector<long long> lens(count);
         for (int r = 0; r < count; ++r) lens[r] = length(r);
         std::nth_element(lens.begin(), lens.begin() + count / 2, lens.end());

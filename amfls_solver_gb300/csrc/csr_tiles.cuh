@@ -1,15 +1,18 @@
 // Tiled CSR products: nnz-balanced warp tasks, one warp per task.
 //
 // A side of the operator (A or its stored transpose) is cut once, on the
-// host, into warp tasks.  Every warp of the grid walks its own tasks (warp
-// w takes tasks w, w + W, ... with W warps in the grid) and no warp waits on
-// another, so the only synchronisation is __syncwarp and an SM keeps many
-// independent tasks in flight.
+// host, into warp tasks listed longest first.  The warps of the grid take
+// them round by round in snake order (round k of W = grid warps: warp w
+// takes task k W + w when k is even, k W + W - 1 - w when k is odd); no warp
+// waits on another, so the only synchronisation is __syncwarp and an SM
+// keeps many independent tasks in flight.  The assignment is static so that
+// each thread adds its rows' epilogue terms in an order fixed by the table.
 //
 // Single-column products (C == 1).  The FP64 pipe of this GPU retires two
 // lanes' FMAs per SM clock and a warp instruction costs the same with one
-// lane active as with 32, so the row sums are laid out to keep all lanes of
-// every FMA busy:
+// lane active as with 32, so on sides whose median row has at most
+// kChainShort nonzeros the row sums are laid out to keep every lane of
+// every FMA busy (chain tables, kChains):
 //   * a chain group is up to 32 rows of (nearly) the same length, at most
 //     kChainMax nonzeros each; lane l sums row l of the group as a
 //     sequential FMA chain from 0 in storage order -- the order of the
@@ -20,22 +23,30 @@
 //     indices (consecutive lanes take consecutive elements of one row), the
 //     gathers x[j], then a transposed store to shared memory from which
 //     each lane reads its own row's next elements without bank conflicts.
-//     Rows of up to kChainShort nonzeros are grouped within windows of
-//     consecutive rows (so neighbouring rows share sectors in time), longer
-//     chain rows by length over the whole side;
+//     A group whose rows hold at most one nonzero takes kFlatRows rows, 8
+//     per lane, straight from registers.  Rows of up to kChainShort
+//     nonzeros are grouped within windows of consecutive rows (so that
+//     neighbouring rows share sectors in time), longer chain rows by length
+//     over the whole side;
 //   * a row longer than kChainMax is one warp task (up to kRowTaskTiles E
 //     nonzeros) or cut into kRowTaskTiles E-element slices.
-// Block products (C = 2..8 columns, X staged row-major so that one gather
-// reads C contiguous doubles) use row blocks: runs of consecutive rows whose
-// nonzeros total at most E (and at most E rows):
+// On sides of longer rows a chain group would need many dependent staging
+// passes, and row blocks are used instead: runs of consecutive rows whose
+// nonzeros total at most E (and at most E rows), with rows longer than E as
+// whole-row tasks or slices:
 //   1. coalesced loads of the tile's values and column indices (E / 32 of
 //      each per lane, all issued before any is used), then the gathers
 //      x[j_e], again all in flight together; values and gathered x go to the
 //      warp's shared-memory buffers, and so do the tile's row offsets;
-//   2. row sums: a group of C lanes takes a row (lane c, column c), each a
-//      sequential FMA chain in storage order (rows of these tiles have at
-//      most E <= kSeqMax nonzeros);
-//   3. results go into the column-major output block.
+//   2. row sums: one column -- lane i takes rows i, i + 32, ... of at most
+//      kSeqMax nonzeros as sequential chains in storage order (bit for bit
+//      the reference's), longer rows of the tile go to 8-lane groups
+//      (strided, fixed butterfly), four rows at a time; C = 2..8 columns (X
+//      staged row-major so that one gather reads C contiguous doubles) -- a
+//      group of C lanes takes a row (lane c, column c), each a sequential
+//      chain (rows of these tiles have at most E = kEC <= kSeqMax nonzeros);
+//   3. results go through the fused epilogue (one column) or into the
+//      column-major output block.
 // A long row (or slice) is streamed through registers by the warp -- E / 32
 // values, indices and gathers per lane in flight per step, lanes strided by
 // element, then a fixed butterfly -- without shared memory.  Slices' partial

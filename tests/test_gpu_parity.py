@@ -124,10 +124,12 @@ def skewed_csr(seed=7, m=6000, n=6000):
     return problems.CsrProblem(m, n, off, col, val, np.zeros(m))
 
 
-def test_csr_tiled_products_long_and_empty_rows(amfls):
-    """Tiled products (row blocks, slices of long rows, empty rows) against
-    the oracle's sequential products within gamma_{2L+2} |A||x|, for 1..11
-    columns, and bit-identical on a repeat."""
+@pytest.mark.parametrize("chains", ["0", "1"])
+def test_csr_tiled_products_long_and_empty_rows(amfls, monkeypatch, chains):
+    """Tiled products (row blocks or chain groups, slices of long rows, empty
+    rows) against the oracle's sequential products within gamma_{2L+2}
+    |A||x|, for 1..11 columns, and bit-identical on a repeat."""
+    monkeypatch.setenv("AMFLS_GB300_CSR_CHAINS", chains)
     prob = skewed_csr()
     op = amfls.DeviceOperator(csr_tensor(prob))
     ref = orc.Operator(prob)
@@ -167,11 +169,14 @@ def chain_csr(seed=11, m=5000, n=700):
     return problems.CsrProblem(m, n, off, col, val, np.zeros(m))
 
 
-def test_csr_single_column_chains_bit_exact(amfls):
+@pytest.mark.parametrize("chains", ["0", "1"])
+def test_csr_single_column_chains_bit_exact(amfls, monkeypatch, chains):
     """Single-column products sum every row (and column) of up to 64
     nonzeros as one FMA chain in storage order from 0, as the reference's
-    SparseCsrOperator::apply / apply_transpose do, so those entries are
-    bit-identical to the oracle's; longer ones are within gamma_{2L+2}."""
+    SparseCsrOperator::apply / apply_transpose do -- in chain groups and in
+    row blocks -- so those entries are bit-identical to the oracle's; longer
+    ones are within gamma_{2L+2}."""
+    monkeypatch.setenv("AMFLS_GB300_CSR_CHAINS", chains)
     prob = chain_csr()
     op = amfls.DeviceOperator(csr_tensor(prob))
     ref = orc.Operator(prob)
@@ -234,8 +239,13 @@ def test_dense_block_products(amfls, layout, s):
 CSR_SOLVES = [n for n in SOLVE_FIXTURES if "dense" not in n and "fixed" not in n]
 
 
+@pytest.mark.parametrize("chains", ["auto", "1"])
 @pytest.mark.parametrize("name", CSR_SOLVES)
-def test_csr_solve_matches_reference(amfls, name):
+def test_csr_solve_matches_reference(amfls, monkeypatch, name, chains):
+    """chains="1" builds chain groups for the short-row sides of these small
+    matrices too (by default only sides of 2^21 nonzeros or more get them)."""
+    if chains != "auto":
+        monkeypatch.setenv("AMFLS_GB300_CSR_CHAINS", chains)
     data, prob = load_golden(name)
     opts = golden_options(data)
     r = amfls.run_amfls(csr_tensor(prob), torch.from_numpy(prob.b).cuda(), **opts)
