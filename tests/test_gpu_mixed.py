@@ -37,8 +37,12 @@ def reduced_bound(absa, x, L, values):
     return 2.0 * (uv + (L + 3) * U32) * (absa @ np.abs(x)) + 1e-300
 
 
+@pytest.mark.parametrize("chains", ["0", "1"])
 @pytest.mark.parametrize("values", ["fp32", "bf16"])
-def test_reduced_csr_products(amfls, values):
+def test_reduced_csr_products(amfls, monkeypatch, values, chains):
+    """Row blocks (chains="0") and chain groups (chains="1") of the shared
+    single-column tables."""
+    monkeypatch.setenv("AMFLS_GB300_CSR_CHAINS", chains)
     prob = skewed_csr(m=3000, n=3000)
     a = prob.to_dense()
     op = amfls.DeviceOperator(csr_tensor(prob))
