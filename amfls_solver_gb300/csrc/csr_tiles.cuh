@@ -180,7 +180,8 @@ tile_product_kernel(const int* __restrict__ off, const int* __restrict__ idx,
     A* xs = reinterpret_cast<A*>(wbase + E * 8);   // E x C gathered x (C > 1)
     int* ro = reinterpret_cast<int*>(wbase + E * 8 + E * C * 8);  // E + 1 row offsets
     // one column: (value, x) pairs, one 16-byte (8-byte for FP32) word each,
-    // so that a chain step reads both with one shared-memory access
+    // so that a chain step or a row sum reads both with one shared-memory
+    // access
     using Pair = std::conditional_t<std::is_same_v<A, double>, double2, float2>;
     Pair* vx = reinterpret_cast<Pair*>(wbase);
     A* vx1 = reinterpret_cast<A*>(wbase);  // pair p: vx1[2 p] value, vx1[2 p + 1] x
