@@ -65,10 +65,17 @@ def _check(rc):
         raise RuntimeError(lib().ref_last_error().decode())
 
 
+_ALGORITHMS = {"amfls": 0, "fixed_rbgk": 1, "lsqr": 2, "lsmr": 3}
+
+
 def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
           failure_probability=1e-6, maximum_epochs=0, maximum_depth=0,
           maximum_auxiliary_width=0, maximum_basis_size=0, seed=0, stream=0,
-          auxiliary_width=4, trace_capacity=4096):
+          auxiliary_width=4, maximum_iterations=0, trace_capacity=4096):
+    """algorithm: amfls, fixed_rbgk, lsqr or lsmr (the last two take
+    regularization, tolerance and maximum_iterations only)."""
+    if algorithm in ("lsqr", "lsmr"):
+        maximum_depth = maximum_iterations
     kind, m, n, off, col, val, nnz, keep = _operator_args(problem)
     b = np.ascontiguousarray(problem.b, dtype=np.float64)
     x = np.zeros(n)
@@ -81,7 +88,7 @@ def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
     status = ctypes.c_int(0)
     reason = ctypes.c_int(0)
     _check(lib().ref_solve(
-        0 if algorithm == "amfls" else 1, kind, m, n, _ptr(off), _ptr(col),
+        _ALGORITHMS[algorithm], kind, m, n, _ptr(off), _ptr(col),
         _ptr(val), nnz, _ptr(b), regularization, tolerance, failure_probability,
         maximum_epochs, maximum_depth, maximum_auxiliary_width,
         maximum_basis_size, seed, stream, auxiliary_width, _ptr(x),

@@ -7,6 +7,8 @@
 // Entry points mirror the reference's own call sites:
 //   solve_amfls          include/amfls/amfls.hpp:22-25
 //   solve_fixed_rbgk     include/amfls/fixed_rbgk.hpp:22-25 (FixedRbgkOptions :8-18)
+//   solve_lsqr           include/amfls/lsqr.hpp:8-18 (LsqrOptions)
+//   solve_lsmr           include/amfls/lsmr.hpp (LsmrOptions, the same three fields)
 //   SparseCsrOperator    src/algorithms/mathematics/operators/sparse_csr_operator.hpp:13-58
 //   RowMajorDenseOperator / DenseOperator (validation_error_model, apply)
 //   gaussian_matrix      src/algorithms/mathematics/random/gaussian.cpp:39-55
@@ -23,6 +25,8 @@
 
 #include "amfls/amfls.hpp"
 #include "amfls/fixed_rbgk.hpp"
+#include "amfls/lsmr.hpp"
+#include "amfls/lsqr.hpp"
 #include "algorithms/mathematics/floating_point_bounds.hpp"
 #include "algorithms/mathematics/operators/dense_operator.hpp"
 #include "algorithms/mathematics/operators/row_major_dense_operator.hpp"
@@ -152,7 +156,7 @@ const char* ref_last_error() { return g_error.c_str(); }
 
 // Returns 0 on success, -1 on an exception (message in ref_last_error()).
 int ref_solve(
-    int algorithm,  // 0 AMFLS, 1 fixed RBGK
+    int algorithm,  // 0 AMFLS, 1 fixed RBGK, 2 LSQR, 3 LSMR (maximum_depth: maximum_iterations)
     int kind, int rows, int cols, const std::int64_t* row_offsets,
     const std::int64_t* column_indices, const double* values,
     std::int64_t nonzeros, const double* b, double regularization,
@@ -179,6 +183,18 @@ int ref_solve(
             o.seed = seed;
             o.stream = stream;
             r = amfls::solve_amfls(*op, b, o);
+        } else if (algorithm == 2) {
+            amfls::LsqrOptions o;
+            o.regularization = regularization;
+            o.tolerance = tolerance;
+            o.maximum_iterations = maximum_depth;
+            r = amfls::solve_lsqr(*op, b, o);
+        } else if (algorithm == 3) {
+            amfls::LsmrOptions o;
+            o.regularization = regularization;
+            o.tolerance = tolerance;
+            o.maximum_iterations = maximum_depth;
+            r = amfls::solve_lsmr(*op, b, o);
         } else {
             amfls::FixedRbgkOptions o;
             o.regularization = regularization;

@@ -32,6 +32,10 @@ def load_golden(name):
 
 def golden_options(data):
     o, i = data["options"], data["int_options"]
+    if int(i[7]) in (2, 3):  # LSQR / LSMR: regularization, tolerance, maximum_iterations
+        return dict(algorithm="lsqr" if int(i[7]) == 2 else "lsmr",
+                    regularization=float(o[0]), tolerance=float(o[1]),
+                    maximum_iterations=int(i[1]))
     opts = dict(regularization=float(o[0]), tolerance=float(o[1]),
                 failure_probability=float(o[2]), seed=int(i[4]), stream=int(i[5]))
     if int(i[7]) == 1:
@@ -44,6 +48,7 @@ def golden_options(data):
 
 
 SOLVE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("solve_*.npz"))
+BASELINE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("baseline_*.npz"))
 
 
 @pytest.fixture(scope="session")

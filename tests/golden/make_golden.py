@@ -49,15 +49,22 @@ def dense_arrays(p):
                 matrix=np.array(p.matrix), b=p.b)
 
 
+ALGORITHM_CODES = {"amfls": 0, "fixed_rbgk": 1, "lsqr": 2, "lsmr": 3}
+
+
 def solve_fixture(name, p, arrays, **opts):
+    """int_options: maximum_epochs, maximum_depth (maximum_iterations for
+    LSQR / LSMR), maximum_auxiliary_width, maximum_basis_size, seed, stream,
+    auxiliary_width, algorithm code."""
     r = ref.solve(p, **opts)
     options = np.array([opts.get("regularization", 0.0), opts.get("tolerance", 1e-8),
                         opts.get("failure_probability", 1e-6)])
-    ints = np.array([opts.get("maximum_epochs", 0), opts.get("maximum_depth", 0),
+    ints = np.array([opts.get("maximum_epochs", 0),
+                     opts.get("maximum_iterations", opts.get("maximum_depth", 0)),
                      opts.get("maximum_auxiliary_width", 0),
                      opts.get("maximum_basis_size", 0), opts.get("seed", 0),
                      opts.get("stream", 0), opts.get("auxiliary_width", 4),
-                     1 if opts.get("algorithm", "amfls") == "fixed_rbgk" else 0],
+                     ALGORITHM_CODES[opts.get("algorithm", "amfls")]],
                     dtype=np.int64)
     save(name, **arrays, options=options, int_options=ints, solution=r["solution"],
          metrics=r["metrics"], counters=r["counters"], trace_float=r["trace_float"],
@@ -156,5 +163,38 @@ def main():
                   seed=3)
 
 
+
+def baselines():
+    """Scalar LSQR and LSMR (src/algorithms/lsqr/lsqr.cpp, src/algorithms/lsmr/lsmr.cpp):
+    well-conditioned least squares and ridge problems that certify, the
+    ill-conditioned CSR problem up to the default iteration limit, an
+    iteration cap, a dense column-major operator and a zero right-hand side."""
+    c1 = problems.scaled_uniform_csr(2000, 500, seed=1)
+    d2 = problems.scaled_dense(600, 80, decades=3.0, seed=5, column_major=True)
+    z = problems.scaled_uniform_csr(200, 50, seed=2)
+    z.b = np.zeros(200)
+    w = problems.scaled_uniform_csr(2000, 500, decades=1.0, noise=1e-3, seed=3)
+    for alg in ("lsqr", "lsmr"):
+        solve_fixture(f"baseline_{alg}_wellcond_ls", w, csr_arrays(w), algorithm=alg,
+                      regularization=0.0, tolerance=1e-8)
+        solve_fixture(f"baseline_{alg}_wellcond_ridge", w, csr_arrays(w), algorithm=alg,
+                      regularization=1e-2, tolerance=1e-10)
+        solve_fixture(f"baseline_{alg}_csr_ls", c1, csr_arrays(c1), algorithm=alg,
+                      regularization=0.0, tolerance=1e-8)
+        solve_fixture(f"baseline_{alg}_csr_ridge", c1, csr_arrays(c1), algorithm=alg,
+                      regularization=1e-4, tolerance=1e-10)
+        solve_fixture(f"baseline_{alg}_csr_cap", c1, csr_arrays(c1), algorithm=alg,
+                      regularization=0.0, tolerance=1e-12, maximum_iterations=25)
+        solve_fixture(f"baseline_{alg}_dense_cm", d2, dense_arrays(d2), algorithm=alg,
+                      regularization=1e-6, tolerance=1e-10)
+        solve_fixture(f"baseline_{alg}_zero_rhs", z, csr_arrays(z), algorithm=alg,
+                      regularization=0.0, tolerance=1e-8)
+
+
 if __name__ == "__main__":
-    main()
+    # no argument: every fixture; "baselines": only the LSQR / LSMR ones
+    if sys.argv[1:] == ["baselines"]:
+        baselines()
+    else:
+        main()
+        baselines()
