@@ -26,6 +26,12 @@ class Options(ctypes.Structure):
                 ("use_graphs", ctypes.c_int)]
 
 
+class BaselineOptions(ctypes.Structure):
+    """amfls_gpu_baseline_options: LsqrOptions / LsmrOptions."""
+    _fields_ = [("regularization", ctypes.c_double), ("tolerance", ctypes.c_double),
+                ("maximum_iterations", ctypes.c_int)]
+
+
 class Result(ctypes.Structure):
     _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("iterations", ctypes.c_int),
                 ("depth", ctypes.c_int), ("auxiliary_width", ctypes.c_int),
@@ -67,7 +73,8 @@ EXPORTED = [
     "amfls_gpu_policy_initial_params", "amfls_gpu_policy_create", "amfls_gpu_policy_destroy",
     "amfls_gpu_policy_forward", "amfls_gpu_policy_gradient", "amfls_gpu_policy_train",
     "amfls_gpu_solve_amfls_controlled", "amfls_gpu_solve_amfls_batch",
-    "amfls_gpu_callback_operator_create",
+    "amfls_gpu_callback_operator_create", "amfls_gpu_default_baseline_options",
+    "amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr",
 ]
 
 POLICY_FEATURES = 11
@@ -114,6 +121,11 @@ def load():
     for name in ("amfls_gpu_solve_amfls", "amfls_gpu_solve_fixed_rbgk"):
         getattr(lib, name).argtypes = [P, P, ctypes.POINTER(Options), P, ctypes.POINTER(Result),
                                        P, P, I, P]
+    lib.amfls_gpu_default_baseline_options.argtypes = [ctypes.POINTER(BaselineOptions)]
+    lib.amfls_gpu_default_baseline_options.restype = None
+    for name in ("amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr"):
+        getattr(lib, name).argtypes = [P, P, ctypes.POINTER(BaselineOptions), P,
+                                       ctypes.POINTER(Result), P, P, I, P]
     lib.amfls_gpu_reduced_operator_create.argtypes = [P, I, P, ctypes.POINTER(P)]
     lib.amfls_gpu_solve_amfls_mixed.argtypes = [P, P, P, ctypes.POINTER(Options), D, I, P,
                                                 ctypes.POINTER(Result), P, P, I, P]

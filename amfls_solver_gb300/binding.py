@@ -33,6 +33,15 @@ RUN_FIXED_RBGK_SCHEMA = (
     "float failure_probability, int auxiliary_width, int maximum_depth, "
     "int maximum_basis_size, int seed, int stream) -> "
     "(Tensor, Tensor, Tensor, Tensor, Tensor, Tensor, int, int)")
+# torch_binding.cpp:522-529
+RUN_LSQR_SCHEMA = (
+    "run_lsqr(Tensor matrix, Tensor b, float regularization, float tolerance, "
+    "int maximum_iterations=0) -> "
+    "(Tensor, Tensor, Tensor, Tensor, Tensor, Tensor, int, int)")
+RUN_LSMR_SCHEMA = (
+    "run_lsmr(Tensor matrix, Tensor b, float regularization, float tolerance, "
+    "int maximum_iterations=0) -> "
+    "(Tensor, Tensor, Tensor, Tensor, Tensor, Tensor, int, int)")
 
 
 @dataclass(frozen=True)
@@ -313,7 +322,9 @@ class DeviceOperator:
 
 # --------------------------------------------------------------- solves ----
 
-def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options: _native.Options):
+def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options):
+    """options: _native.Options (amfls, fixed_rbgk) or _native.BaselineOptions
+    (lsqr, lsmr)."""
     lib = _native.load()
     if b.device != op.device:
         raise ValueError("matrix and b must be on the same CUDA device")
@@ -322,7 +333,7 @@ def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options: _na
     res = _native.Result()
     tf = np.zeros((TRACE_CAPACITY, 29))
     ti = np.zeros((TRACE_CAPACITY, 4), dtype=np.int64)
-    fn = lib.amfls_gpu_solve_amfls if algorithm == "amfls" else lib.amfls_gpu_solve_fixed_rbgk
+    fn = getattr(lib, f"amfls_gpu_solve_{algorithm}")
     with torch.cuda.device(b.device):
         _native.check(fn(op.handle, b.data_ptr(), ctypes.byref(options), x.data_ptr(),
                          ctypes.byref(res), tf.ctypes.data, ti.ctypes.data, TRACE_CAPACITY,
@@ -495,7 +506,30 @@ def _run_fixed_rbgk_impl(matrix, b, regularization, tolerance, failure_probabili
     return _solve_raw("fixed_rbgk", op, b, o)
 
 
+def _run_baseline_impl(algorithm, matrix, b, regularization, tolerance, maximum_iterations=0):
+    _check_inputs(matrix, b)
+    op = DeviceOperator(matrix)
+    o = _native.BaselineOptions()
+    _native.load().amfls_gpu_default_baseline_options(ctypes.byref(o))
+    o.regularization = float(regularization)
+    o.tolerance = float(tolerance)
+    o.maximum_iterations = int(maximum_iterations)
+    return _solve_raw(algorithm, op, b, o)
+
+
+def _run_lsqr_impl(matrix, b, regularization, tolerance, maximum_iterations=0):
+    return _run_baseline_impl("lsqr", matrix, b, regularization, tolerance, maximum_iterations)
+
+
+def _run_lsmr_impl(matrix, b, regularization, tolerance, maximum_iterations=0):
+    return _run_baseline_impl("lsmr", matrix, b, regularization, tolerance, maximum_iterations)
+
+
 _LIBS = []
+_OPS = {"run_amfls": (RUN_AMFLS_SCHEMA, "_run_amfls_impl"),
+        "run_fixed_rbgk": (RUN_FIXED_RBGK_SCHEMA, "_run_fixed_rbgk_impl"),
+        "run_lsqr": (RUN_LSQR_SCHEMA, "_run_lsqr_impl"),
+        "run_lsmr": (RUN_LSMR_SCHEMA, "_run_lsmr_impl")}
 
 
 def _op_exists(name: str) -> bool:
@@ -507,21 +541,21 @@ def _op_exists(name: str) -> bool:
 
 
 def register_torch_ops() -> None:
-    """Register torch.ops.amfls.{run_amfls, run_fixed_rbgk} for CUDA tensors."""
+    """Register torch.ops.amfls.{run_amfls, run_fixed_rbgk, run_lsqr, run_lsmr}
+    for CUDA tensors (reference: torch_binding.cpp:511-611)."""
     if _LIBS:
         return
-    defined = {n: _op_exists(n) for n in ("run_amfls", "run_fixed_rbgk")}
+    defined = {n: _op_exists(n) for n in _OPS}
     if not all(defined.values()):
         lib_def = torch.library.Library("amfls", "FRAGMENT")
-        if not defined["run_amfls"]:
-            lib_def.define(RUN_AMFLS_SCHEMA)
-        if not defined["run_fixed_rbgk"]:
-            lib_def.define(RUN_FIXED_RBGK_SCHEMA)
+        for name, (schema, _) in _OPS.items():
+            if not defined[name]:
+                lib_def.define(schema)
         _LIBS.append(lib_def)
     lib_impl = torch.library.Library("amfls", "IMPL")
     for key in ("CUDA", "SparseCsrCUDA"):
-        lib_impl.impl("run_amfls", _run_amfls_impl, key)
-        lib_impl.impl("run_fixed_rbgk", _run_fixed_rbgk_impl, key)
+        for name, (_, impl) in _OPS.items():
+            lib_impl.impl(name, globals()[impl], key)
     _LIBS.append(lib_impl)
 
 
@@ -608,3 +642,21 @@ def run_fixed_rbgk(matrix: torch.Tensor, b: torch.Tensor, *, auxiliary_width: in
         maximum_depth, maximum_basis_size,
         _canonical_uint64_to_int64_transport(seed, "seed"),
         _canonical_uint64_to_int64_transport(stream, "stream")))
+
+
+def run_lsqr(matrix: torch.Tensor, b: torch.Tensor, *, regularization: float = 0.0,
+             tolerance: float = 1e-8, maximum_iterations: int = 0) -> SolveResult:
+    """Scalar LSQR, every checkpoint certified (reference: binding.py:325-342)."""
+    _check_inputs(matrix, b)
+    register_torch_ops()
+    return _decode(torch.ops.amfls.run_lsqr(matrix, b, regularization, tolerance,
+                                            maximum_iterations))
+
+
+def run_lsmr(matrix: torch.Tensor, b: torch.Tensor, *, regularization: float = 0.0,
+             tolerance: float = 1e-8, maximum_iterations: int = 0) -> SolveResult:
+    """Scalar LSMR, every checkpoint certified (reference: binding.py:345-362)."""
+    _check_inputs(matrix, b)
+    register_torch_ops()
+    return _decode(torch.ops.amfls.run_lsmr(matrix, b, regularization, tolerance,
+                                            maximum_iterations))

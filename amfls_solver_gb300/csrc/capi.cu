@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/amfls_gpu.h"
+#include "baselines.hpp"
 #include "batch.hpp"
 #include "callback_operator.hpp"
 #include "common.cuh"
@@ -130,6 +131,14 @@ void amfls_gpu_default_options(amfls_gpu_options* o) {
     o->use_graphs = 1;
 }
 
+void amfls_gpu_default_baseline_options(amfls_gpu_baseline_options* o) {
+    if (o == nullptr) return;
+    std::memset(o, 0, sizeof(*o));
+    o->regularization = 0.0;
+    o->tolerance = 1e-8;
+    o->maximum_iterations = 0;
+}
+
 const char* amfls_gpu_last_error(void) { return g_last_error.c_str(); }
 
 int amfls_gpu_csr_operator_create(int rows, int cols, const int64_t* d_row_offsets,
@@ -250,6 +259,39 @@ int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
         if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
         const auto r = amfls_gpu::solve_fixed_rbgk(deref(op), d_b, to_options(options),
                                                    d_solution, as_stream(stream));
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+    });
+}
+
+static amfls_gpu::BaselineOptions to_baseline_options(const amfls_gpu_baseline_options* o) {
+    if (o == nullptr) throw std::invalid_argument("options must not be null");
+    amfls_gpu::BaselineOptions b;
+    b.regularization = o->regularization;
+    b.tolerance = o->tolerance;
+    b.maximum_iterations = o->maximum_iterations;
+    return b;
+}
+
+int amfls_gpu_solve_lsqr(const amfls_gpu_operator* op, const double* d_b,
+                         const amfls_gpu_baseline_options* options, double* d_solution,
+                         amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                         int trace_capacity, void* stream) {
+    return guarded([&] {
+        if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
+        const auto r = amfls_gpu::solve_lsqr(deref(op), d_b, to_baseline_options(options),
+                                             d_solution, as_stream(stream));
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+    });
+}
+
+int amfls_gpu_solve_lsmr(const amfls_gpu_operator* op, const double* d_b,
+                         const amfls_gpu_baseline_options* options, double* d_solution,
+                         amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                         int trace_capacity, void* stream) {
+    return guarded([&] {
+        if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
+        const auto r = amfls_gpu::solve_lsmr(deref(op), d_b, to_baseline_options(options),
+                                             d_solution, as_stream(stream));
         export_result(r, result, trace_float, trace_int, trace_capacity);
     });
 }

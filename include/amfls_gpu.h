@@ -91,8 +91,18 @@ typedef struct {
     long long kernel_launches; /* GPU kernels the solve ran (not part of the reference) */
 } amfls_gpu_result;
 
+/* LsqrOptions (lsqr.hpp:8-12) and LsmrOptions (lsmr.hpp): the same fields. */
+typedef struct {
+    double regularization;  /* lambda >= 0 (damp^2) */
+    double tolerance;       /* (0, 1) */
+    int maximum_iterations; /* 0 = min(rows, cols) */
+} amfls_gpu_baseline_options;
+
 /* Sets the reference's defaults (amfls.hpp:10-20; fixed_rbgk.hpp:8-18). */
 void amfls_gpu_default_options(amfls_gpu_options* options);
+
+/* Sets LsqrOptions' / LsmrOptions' defaults (lambda 0, tol 1e-8, 0 iterations). */
+void amfls_gpu_default_baseline_options(amfls_gpu_baseline_options* options);
 
 /* Message of the calling thread's last error ("" if none). */
 const char* amfls_gpu_last_error(void);
@@ -168,6 +178,20 @@ int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
                                const amfls_gpu_options* options, double* d_solution,
                                amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
                                int trace_capacity, void* stream);
+
+/* solve_lsqr (lsqr.hpp:14-17; lsqr.cpp:84-281) and solve_lsmr (lsmr.hpp;
+ * lsmr.cpp:112-351): scalar LSQR / LSMR on the same operators, every
+ * checkpoint certified by the same validation as AMFLS; result, trace and
+ * error conventions as amfls_gpu_solve_amfls (iterations = depth = basis
+ * rank = the last certified iteration, auxiliary width 0). */
+int amfls_gpu_solve_lsqr(const amfls_gpu_operator* op, const double* d_b,
+                         const amfls_gpu_baseline_options* options, double* d_solution,
+                         amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                         int trace_capacity, void* stream);
+int amfls_gpu_solve_lsmr(const amfls_gpu_operator* op, const double* d_b,
+                         const amfls_gpu_baseline_options* options, double* d_solution,
+                         amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
+                         int trace_capacity, void* stream);
 
 /* Mixed-precision form (no counterpart in the reference, whose solver is
  * FP64 throughout).

@@ -85,6 +85,19 @@ def test_mixed_entry_points_reject_bad_arguments(lib):
     assert rc == 1 and b"operator must not be null" in lib.amfls_gpu_last_error()
 
 
+def test_lsqr_lsmr_entry_points_reject_bad_arguments(lib):
+    o = _native.BaselineOptions()
+    lib.amfls_gpu_default_baseline_options(ctypes.byref(o))
+    assert (o.regularization, o.tolerance, o.maximum_iterations) == (0.0, 1e-8, 0)
+    res = _native.Result()
+    for name in ("amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr"):
+        fn = getattr(lib, name)
+        rc = fn(None, None, ctypes.byref(o), None, ctypes.byref(res), None, None, 0, None)
+        assert rc == 1 and b"solution must not be null" in lib.amfls_gpu_last_error()
+        rc = fn(None, None, None, ctypes.c_void_p(16), ctypes.byref(res), None, None, 0, None)
+        assert rc == 1 and b"must not be null" in lib.amfls_gpu_last_error()
+
+
 def test_callback_operator_needs_both_products(lib):
     cb = _native.Callbacks()
     handle = ctypes.c_void_p()
