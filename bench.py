@@ -20,6 +20,9 @@ mixed     time-to-tol of the mixed-precision form (FP32 inner solves refined
           in FP64, certified by the FP64 validation) next to plain FP64 on
           the 20000 x 5000 CSR problem, and the mixed form on the headline
           workload;
+baselines AMFLS against the scalar LSQR and LSMR baselines on the 20000 x 5000
+          CSR problem at its tolerance (seconds, status, iterations,
+          certificate), the reference's own comparison;
 batched   problems/s, p50 and p99 per-problem time of batched solves on a
           bounded sample of the uneven 256-problem CSR workload (sizes as
           described in the line), 16 workers against 1;
@@ -69,6 +72,8 @@ def parse():
     ap.add_argument("--spmm", type=int, default=1,
                     help="0 skips the CSR SpMM GB/s measurement on the 2M x 500k matrix")
     ap.add_argument("--mixed", type=int, default=1, help="0 skips the mixed-precision leg")
+    ap.add_argument("--baselines", type=int, default=1,
+                    help="0 skips the AMFLS vs LSQR / LSMR leg on the 20000 x 5000 CSR problem")
     ap.add_argument("--batched", type=int, default=48,
                     help="problems in the batched leg's sample (0 skips it)")
     return ap.parse_args()
@@ -271,6 +276,52 @@ def spmm_measurement(dev, stream, peak):
                          "frac": nbytes / t / 1e9 / peak, "algorithmic_bytes": nbytes}
         out[f"s{cols}"] = res
     return out
+
+
+def baselines_measurement(dev):
+    """AMFLS against the scalar LSQR and LSMR baselines (the reference's own
+    comparison) on the 20000 x 5000 CSR problem at its tolerance: host wall
+    clock around each synchronous C-ABI solve on one prebuilt operator, after
+    one warm-up each, with status, iterations and certificate.  An error is
+    reported in the object rather than raised."""
+    import ctypes
+    import torch
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import binding, _native
+
+    try:
+        prob, opts = make_workload("csr_20000x5000")
+        a = torch.sparse_csr_tensor(torch.from_numpy(prob.row_offsets),
+                                    torch.from_numpy(prob.column_indices),
+                                    torch.from_numpy(prob.values),
+                                    size=(prob.rows, prob.cols)).to(dev)
+        op = amfls.DeviceOperator(a)
+        b = torch.from_numpy(prob.b).to(dev)
+        reg, tol = opts["regularization"], opts["tolerance"]
+        o = _native.default_options()
+        for k, v in opts.items():
+            setattr(o, k, v)
+        ob = _native.BaselineOptions()
+        _native.load().amfls_gpu_default_baseline_options(ctypes.byref(ob))
+        ob.regularization, ob.tolerance = reg, tol
+        out = {"workload": "csr_20000x5000", "tolerance": tol, "regularization": reg,
+               "maximum_iterations": min(prob.rows, prob.cols)}
+        for name, options in (("amfls", o), ("lsqr", ob), ("lsmr", ob)):
+            def run():
+                return binding._decode(binding._solve_raw(name, op, b, options))
+            run()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = run()
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+            out[name] = {"s": t, "status": r.status, "stop_reason": r.stop_reason,
+                         "iterations": r.depth,
+                         "certificate": r.relative_energy_error_upper_bound if reg > 0
+                         else r.backward_error_upper_bound}
+        return out
+    except Exception as e:  # reported, not fatal to the bench line
+        return {"error": f"{type(e).__name__}: {e}"}
 
 
 def mixed_measurement(dev, headline_op, headline_b, headline_opts):
@@ -526,6 +577,7 @@ def run_ours(args, world, rank, local):
 
     spmm = spmm_measurement(dev, stream, peak) if args.spmm else None
     mixed = mixed_measurement(dev, op, b_dev, opts) if args.mixed and rank == 0 else None
+    baselines = baselines_measurement(dev) if args.baselines and rank == 0 else None
     batched = batched_measurement(dev, args.batched) if args.batched > 0 and rank == 0 else None
 
     if rank != 0:
@@ -547,7 +599,7 @@ def run_ours(args, world, rank, local):
                        "depth": depth, "status": list(status), "parallelism": "replicas"},
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": roof, "spmm": spmm, "mixed": mixed, "batched": batched,
+            "roofline": roof, "spmm": spmm, "mixed": mixed, "baselines": baselines, "batched": batched,
             "cpu_baseline": cpu, "clocks": clocks.summary(),
             "gpu_launches": launches * args.steps}
     print(json.dumps(line), flush=True)
