@@ -22,6 +22,7 @@ from .binding import (
     run_lsmr,
     run_lsqr,
     solve_amfls,
+    solve_amfls_replay,
 )
 
 __all__ = [
@@ -36,4 +37,5 @@ __all__ = [
     "run_lsmr",
     "run_lsqr",
     "solve_amfls",
+    "solve_amfls_replay",
 ]

@@ -74,7 +74,7 @@ EXPORTED = [
     "amfls_gpu_policy_forward", "amfls_gpu_policy_gradient", "amfls_gpu_policy_train",
     "amfls_gpu_solve_amfls_controlled", "amfls_gpu_solve_amfls_batch",
     "amfls_gpu_callback_operator_create", "amfls_gpu_default_baseline_options",
-    "amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr",
+    "amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr", "amfls_gpu_solve_amfls_replay",
 ]
 
 POLICY_FEATURES = 11
@@ -143,6 +143,8 @@ def load():
     lib.amfls_gpu_solve_amfls_controlled.argtypes = [P, P, ctypes.POINTER(Options), P, D, U64,
                                                      P, I, P, P, ctypes.POINTER(Result), P, P,
                                                      I, P]
+    lib.amfls_gpu_solve_amfls_replay.argtypes = [P, P, ctypes.POINTER(Options), P, I, P, I, P,
+                                                 P, P, ctypes.POINTER(Result), P, P, I, P]
     _lib = lib
     return lib
 

@@ -375,6 +375,55 @@ def solve_amfls(op: DeviceOperator, b: torch.Tensor, *, regularization: float = 
     return _decode(_solve_raw("amfls", op, b, o))
 
 
+def solve_amfls_replay(op: DeviceOperator, b: torch.Tensor, replay, *,
+                       regularization: float = 0.0, tolerance: float = 1e-8,
+                       failure_probability: float = 1e-6, maximum_epochs: int = 0,
+                       maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
+                       maximum_basis_size: int = 0, seed: int = 0, stream: int = 0):
+    """AMFLS in schedule-replay mode: the width decisions at the controller's
+    decision sites (amfls.cpp:323-354) take the candidate bits in `replay`
+    (a sequence of 0/1) instead of the timing-driven cost gate's, so a
+    widening solve recorded on the reference is reproduced whatever the
+    timings.  Returns (SolveResult, decisions, overrun): the bit taken at
+    every decision site and the number of sites beyond the list.  A test
+    mode; no counterpart in the reference's API."""
+    if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
+        raise ValueError("b must be a float64 CUDA vector of length rows on the operator's device")
+    o = _native.default_options()
+    o.regularization = float(regularization)
+    o.tolerance = float(tolerance)
+    o.failure_probability = float(failure_probability)
+    o.maximum_epochs = int(maximum_epochs)
+    o.maximum_depth = int(maximum_depth)
+    o.maximum_auxiliary_width = int(maximum_auxiliary_width)
+    o.maximum_basis_size = int(maximum_basis_size)
+    o.seed = _uint64(seed)
+    o.stream = _uint64(stream)
+    rp = np.ascontiguousarray(np.asarray(list(replay), dtype=np.int32))
+    cap = 1 << 16
+    dec = np.zeros(cap, dtype=np.int32)
+    count = ctypes.c_int(0)
+    over = ctypes.c_longlong(0)
+    b = b.contiguous()
+    x = torch.empty(op.cols, dtype=torch.float64, device=b.device)
+    res = _native.Result()
+    tf = np.zeros((TRACE_CAPACITY, 29))
+    ti = np.zeros((TRACE_CAPACITY, 4), dtype=np.int64)
+    with torch.cuda.device(b.device):
+        _native.check(_native.load().amfls_gpu_solve_amfls_replay(
+            op.handle, b.data_ptr(), ctypes.byref(o), rp.ctypes.data, int(rp.shape[0]),
+            dec.ctypes.data, cap, ctypes.byref(count), ctypes.byref(over), x.data_ptr(),
+            ctypes.byref(res), tf.ctypes.data, ti.ctypes.data, TRACE_CAPACITY,
+            _stream_handle(b.device)))
+    rows = min(res.trace_rows, TRACE_CAPACITY)
+    result = _decode((x, torch.tensor(list(res.metrics), dtype=torch.float64),
+                      torch.tensor(list(res.counters), dtype=torch.int64),
+                      torch.tensor(list(res.timings), dtype=torch.float64),
+                      torch.from_numpy(tf[:rows].copy()), torch.from_numpy(ti[:rows].copy()),
+                      int(res.status), int(res.stop_reason)))
+    return result, dec[:min(count.value, cap)].copy(), int(over.value)
+
+
 def run_amfls_batch(problems, *, workers: int = 16, regularization=0.0, tolerance=1e-8,
                     failure_probability: float = 1e-6, maximum_epochs: int = 0,
                     maximum_depth: int = 0, maximum_auxiliary_width: int = 0,

@@ -444,6 +444,36 @@ int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double*
     });
 }
 
+int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b,
+                                 const amfls_gpu_options* options, const int* replay,
+                                 int replay_count, int* decisions, int decision_capacity,
+                                 int* decision_count, long long* replay_overrun,
+                                 double* d_solution, amfls_gpu_result* result,
+                                 double* trace_float, int64_t* trace_int, int trace_capacity,
+                                 void* stream) {
+    return guarded([&] {
+        if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
+        if (replay_count > 0 && replay == nullptr)
+            throw std::invalid_argument("replay list must not be null");
+        if (decision_capacity < 0 || (decision_capacity > 0 && decisions == nullptr))
+            throw std::invalid_argument("decision buffer is invalid");
+        std::vector<int> sites;
+        long long overrun = 0;
+        amfls_gpu::WidthControl ctl;
+        ctl.replay = replay;
+        ctl.replay_count = replay_count < 0 ? -1 : replay_count;
+        ctl.sites = &sites;
+        ctl.overrun = &overrun;
+        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, to_options(options), d_solution,
+                                              as_stream(stream), &ctl);
+        export_result(r, result, trace_float, trace_int, trace_capacity);
+        const int n = std::min<int>(decision_capacity, (int)sites.size());
+        for (int i = 0; i < n; ++i) decisions[i] = sites[i];
+        if (decision_count) *decision_count = (int)sites.size();
+        if (replay_overrun) *replay_overrun = overrun;
+    });
+}
+
 int amfls_gpu_solve_amfls_batch(int count, const amfls_gpu_operator* const* ops,
                                 const double* const* d_b, const amfls_gpu_options* options,
                                 double* const* d_solutions, amfls_gpu_result* results,

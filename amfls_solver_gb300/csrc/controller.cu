@@ -578,7 +578,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
 
     History hist;
     Plan plan;
-    int epoch = 0;
+    int epoch = 0, replay_sites = 0;
     std::uint64_t generated = 0;
     bool feedback = false;
     int fb_target = 0, stage_rank = 0, stage_origin = 0, stage_target = 0;
@@ -628,7 +628,17 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
                                         ws.basis_rank(), ws.basis_limit(), frontier, hist,
                                         op.relative_block_product_cost(frontier),
                                         op.relative_block_product_cost(tw));
-            bool widen = d.candidate;
+            // the candidate bit, or the replayed one in schedule-replay mode
+            bool candidate = d.candidate;
+            if (control && control->replay_count >= 0) {
+                if (replay_sites < control->replay_count)
+                    candidate = control->replay[replay_sites] != 0;
+                else if (control->overrun)
+                    ++*control->overrun;
+                ++replay_sites;
+            }
+            if (control && control->sites) control->sites->push_back(candidate ? 1 : 0);
+            bool widen = candidate;
             if (control) {
                 DecisionRecord rec{};
                 width_features(rec.features, interval_cert, tol, hist, plan,
@@ -662,7 +672,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
             }
             if (widen) {
                 requested = inc;
-                if (!horizon_active && d.candidate) req_horizon = d.matched_horizon;
+                if (!horizon_active && candidate) req_horizon = d.matched_horizon;
             }
         }
         if (horizon_active && ready && requested == 0) plan = Plan{};

@@ -74,11 +74,22 @@ struct SolveResult {
 // and a log of every decision with its features and the certificate's rate
 // of decrease until the next decision.  Without it (or with all fields
 // empty) solve_amfls is the reference's controller.
+//
+// Schedule replay: with replay_count >= 0 the heuristic's candidate bit at
+// the n-th decision site (amfls.cpp:323-354) is replaced by replay[n]; sites
+// beyond the list keep the heuristic's bit and are counted in *overrun.  The
+// bit is the only part of a width decision that depends on measured seconds,
+// so replaying the reference's recorded bits reproduces its widening solve
+// whatever the timings.  `sites` (if set) receives every site's bit in order.
 struct WidthControl {
     const WidthPolicy* policy = nullptr;
     double exploration = 0.0;
     std::uint64_t exploration_seed = 0;
     std::vector<DecisionRecord>* log = nullptr;
+    const int* replay = nullptr;
+    int replay_count = -1;
+    std::vector<int>* sites = nullptr;
+    long long* overrun = nullptr;
 };
 
 SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const SolveOptions& options,

@@ -276,6 +276,27 @@ int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double*
                                      double* trace_float, int64_t* trace_int, int trace_capacity,
                                      void* stream);
 
+/* solve_amfls in schedule-replay mode (a test mode; the reference's
+ * controller is amfls.cpp:57-661).  The controller's width decisions at its
+ * decision sites (amfls.cpp:323-354, in order) take the candidate bits
+ * replay[0 .. replay_count) instead of the bits its timing-driven cost gate
+ * computes (amfls_internal.hpp:236-552); every other quantity of a decision
+ * (increment, matched horizon) is computed as usual.  The bit is the only
+ * timing-dependent part of a decision, so replaying the bits recorded from a
+ * reference run reproduces that run's widening path on this GPU.  Sites
+ * beyond the list keep their own bit and are counted in *replay_overrun;
+ * replay_count < 0 replays nothing (the plain controller).  decisions
+ * (capacity decision_capacity, may be NULL when 0) receives the bit taken at
+ * every site and *decision_count the number of sites.  Other conventions as
+ * amfls_gpu_solve_amfls. */
+int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b,
+                                 const amfls_gpu_options* options, const int* replay,
+                                 int replay_count, int* decisions, int decision_capacity,
+                                 int* decision_count, long long* replay_overrun,
+                                 double* d_solution, amfls_gpu_result* result,
+                                 double* trace_float, int64_t* trace_int, int trace_capacity,
+                                 void* stream);
+
 /* Batched AMFLS (no counterpart in the reference): `count` independent
  * problems, problem i = (ops[i], d_b[i], options[i]) with its solution in
  * d_solutions[i] (a distinct operator per problem: an operator's products

@@ -1073,19 +1073,28 @@ def _certificate(r, reg):
 
 def solve_amfls(problem, regularization=0.0, tolerance=1e-8, failure_probability=1e-6,
                 maximum_epochs=0, maximum_depth=0, maximum_auxiliary_width=0,
-                maximum_basis_size=0, seed=0, stream=0):
+                maximum_basis_size=0, seed=0, stream=0, replay=None):
     """amfls.cpp:57-661. Returns the result dict in the torch binding's layout."""
     op = Operator(problem)
     b = np.ascontiguousarray(problem.b, dtype=np.float64)
     return solve_amfls_operator(op, b, regularization, tolerance, failure_probability,
                                 maximum_epochs, maximum_depth, maximum_auxiliary_width,
-                                maximum_basis_size, seed, stream)
+                                maximum_basis_size, seed, stream, replay=replay)
 
 
 def solve_amfls_operator(op, b, regularization=0.0, tolerance=1e-8, failure_probability=1e-6,
                          maximum_epochs=0, maximum_depth=0, maximum_auxiliary_width=0,
-                         maximum_basis_size=0, seed=0, stream=0):
+                         maximum_basis_size=0, seed=0, stream=0, replay=None):
+    """The controller of amfls.cpp:57-661.  The result also carries
+    ``decisions``: the candidate bit of every width decision taken at the
+    reference's decision sites (amfls.cpp:323-354).  ``replay`` (a sequence
+    of 0/1) substitutes those bits in order for the timing-driven ones, the
+    schedule-replay mode that makes widening solves reproducible; sites
+    beyond the list keep their own decision and are counted in
+    ``replay_overrun``."""
     reg, tol = regularization, tolerance
+    decisions = []
+    overrun = 0
     validate_common_inputs(op, b, reg, tol)
     if not math.isfinite(failure_probability) or not (0.0 < failure_probability < 1.0):
         raise ValueError("failure_probability must lie strictly between zero and one")
@@ -1130,7 +1139,10 @@ def solve_amfls_operator(op, b, regularization=0.0, tolerance=1e-8, failure_prob
         final["trace"] = list(trace)
         stats.total_seconds = time.perf_counter() - t_start
         final["statistics"] = stats.copy()
-        return pack(final, op.cols)
+        out = pack(final, op.cols)
+        out["decisions"] = np.array(decisions, dtype=np.int32)
+        out["replay_overrun"] = overrun
+        return out
 
     def finish_at_limit(status, reason):
         return finish(st["result"] if reg > 0.0 else st["best"], status, reason)
@@ -1208,6 +1220,12 @@ def solve_amfls_operator(op, b, regularization=0.0, tolerance=1e-8, failure_prob
                                       ws.basis_limit, frontier, hist,
                                       op.relative_block_product_cost(frontier),
                                       op.relative_block_product_cost(tw))
+            if replay is not None:
+                if len(decisions) < len(replay):
+                    d.candidate = bool(replay[len(decisions)])
+                else:
+                    overrun += 1
+            decisions.append(1 if d.candidate else 0)
             if d.candidate:
                 requested = inc
                 if not horizon_active:

@@ -39,6 +39,10 @@ def lib():
         _lib.ref_gaussian_matrix.argtypes = [_I, _I, _U64, _U64, _U64, _P]
         _lib.ref_norm_interval.argtypes = [_P, _I64, _P]
         _lib.ref_norm_interval.restype = None
+        _lib.ref_set_width_replay.argtypes = [_P, _I]
+        _lib.ref_set_width_replay.restype = None
+        _lib.ref_width_decisions.argtypes = [_P, _P, _I, ctypes.POINTER(ctypes.c_longlong)]
+        _lib.ref_width_decisions.restype = _I
     return _lib
 
 
@@ -71,9 +75,16 @@ _ALGORITHMS = {"amfls": 0, "fixed_rbgk": 1, "lsqr": 2, "lsmr": 3}
 def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
           failure_probability=1e-6, maximum_epochs=0, maximum_depth=0,
           maximum_auxiliary_width=0, maximum_basis_size=0, seed=0, stream=0,
-          auxiliary_width=4, maximum_iterations=0, trace_capacity=4096):
+          auxiliary_width=4, maximum_iterations=0, trace_capacity=4096, replay=None):
     """algorithm: amfls, fixed_rbgk, lsqr or lsmr (the last two take
-    regularization, tolerance and maximum_iterations only)."""
+    regularization, tolerance and maximum_iterations only).
+
+    The AMFLS result carries ``decisions`` (the candidate bit of every width
+    decision the controller took, amfls.cpp:323-354), ``horizons`` (their
+    matched horizons) and ``replay_overrun``.  ``replay`` (a sequence of 0/1)
+    makes the controller take those decisions in order instead of its
+    timing-driven ones (sites beyond the list keep the reference's choice and
+    are counted in ``replay_overrun``)."""
     if algorithm in ("lsqr", "lsmr"):
         maximum_depth = maximum_iterations
     kind, m, n, off, col, val, nnz, keep = _operator_args(problem)
@@ -87,6 +98,8 @@ def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
     rows = ctypes.c_int(0)
     status = ctypes.c_int(0)
     reason = ctypes.c_int(0)
+    rp = np.ascontiguousarray(np.asarray(replay if replay is not None else [], dtype=np.int32))
+    lib().ref_set_width_replay(_ptr(rp), rp.shape[0] if replay is not None else -1)
     _check(lib().ref_solve(
         _ALGORITHMS[algorithm], kind, m, n, _ptr(off), _ptr(col),
         _ptr(val), nnz, _ptr(b), regularization, tolerance, failure_probability,
@@ -95,10 +108,18 @@ def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
         _ptr(metrics), _ptr(counters), _ptr(timings), _ptr(tf), _ptr(ti),
         trace_capacity, ctypes.byref(rows), ctypes.byref(status),
         ctypes.byref(reason)))
+    lib().ref_set_width_replay(None, -1)
     r = min(rows.value, trace_capacity)
+    cap = 1 << 16
+    dec = np.zeros(cap, dtype=np.int32)
+    hor = np.zeros(cap, dtype=np.int32)
+    over = ctypes.c_longlong(0)
+    nd = lib().ref_width_decisions(_ptr(dec), _ptr(hor), cap, ctypes.byref(over))
     return dict(solution=x, metrics=metrics, counters=counters, timings=timings,
                 trace_float=tf[:r].copy(), trace_int=ti[:r].copy(),
-                status=status.value, stop_reason=reason.value)
+                status=status.value, stop_reason=reason.value,
+                decisions=dec[:min(nd, cap)].copy(), horizons=hor[:min(nd, cap)].copy(),
+                replay_overrun=int(over.value))
 
 
 def apply(problem, x, transpose=False):

@@ -13,6 +13,7 @@
 //   RowMajorDenseOperator / DenseOperator (validation_error_model, apply)
 //   gaussian_matrix      src/algorithms/mathematics/random/gaussian.cpp:39-55
 //   fp::norm_interval    src/algorithms/mathematics/floating_point_bounds.hpp:325-376
+//   width decisions      amfls.cpp:323-354 (recorded / replayed through ref_hooks.hpp)
 // The result packing follows the layout of bindings/torch/result_tensors.hpp:24-156
 // (21 metrics, 36 counters, 9 timings, 29 + 4 trace columns).
 #include <cstdint>
@@ -36,6 +37,33 @@
 namespace {
 
 thread_local std::string g_error;
+
+// Width decisions of the last AMFLS solve (candidate bit, matched horizon)
+// and, when g_replay_active, the candidate bits to substitute in order.
+std::vector<int> g_decisions;
+std::vector<int> g_horizons;
+std::vector<int> g_replay;
+bool g_replay_active = false;
+std::size_t g_replay_position = 0;
+long long g_replay_overrun = 0;
+
+}  // namespace
+
+amfls::detail::WidthDecision amfls::detail::ref_hook_width_decision(WidthDecision decision) {
+    if (g_replay_active) {
+        if (g_replay_position < g_replay.size()) {
+            decision.candidate = g_replay[g_replay_position] != 0;
+        } else {
+            ++g_replay_overrun;  // more decision sites than recorded: keep the reference's
+        }
+        ++g_replay_position;
+    }
+    g_decisions.push_back(decision.candidate ? 1 : 0);
+    g_horizons.push_back(decision.matched_horizon);
+    return decision;
+}
+
+namespace {
 
 struct OperatorSpec {
     int kind;  // 0 CSR, 1 row-major dense, 2 column-major dense
@@ -154,6 +182,25 @@ extern "C" {
 
 const char* ref_last_error() { return g_error.c_str(); }
 
+// Replay list for the next AMFLS solves (count < 0 switches replay off).
+void ref_set_width_replay(const int* decisions, int count) {
+    g_replay_active = count >= 0;
+    g_replay.assign(decisions, decisions + (count > 0 ? count : 0));
+}
+
+// Decisions of the last solve: candidate bits and matched horizons (up to
+// `capacity` each); returns the number of decision sites, and the count of
+// sites beyond the replay list in *overrun.
+int ref_width_decisions(int* decisions, int* horizons, int capacity, long long* overrun) {
+    const int n = static_cast<int>(g_decisions.size());
+    for (int i = 0; i < n && i < capacity; ++i) {
+        decisions[i] = g_decisions[i];
+        horizons[i] = g_horizons[i];
+    }
+    *overrun = g_replay_overrun;
+    return n;
+}
+
 // Returns 0 on success, -1 on an exception (message in ref_last_error()).
 int ref_solve(
     int algorithm,  // 0 AMFLS, 1 fixed RBGK, 2 LSQR, 3 LSMR (maximum_depth: maximum_iterations)
@@ -167,6 +214,10 @@ int ref_solve(
     double* timings, double* trace_float, std::int64_t* trace_int,
     int trace_capacity, int* trace_rows, int* status, int* stop_reason) {
     try {
+        g_decisions.clear();
+        g_horizons.clear();
+        g_replay_position = 0;
+        g_replay_overrun = 0;
         const OperatorSpec spec{kind, rows, cols, row_offsets, column_indices,
                                 values, nonzeros};
         auto op = make_operator(spec);

@@ -47,7 +47,31 @@ def golden_options(data):
     return opts
 
 
+def load_replay(name):
+    """A schedule-replay fixture and its regenerated problem.  The problem is
+    rebuilt from the seeded generator the fixture names; the SHA-256 of the
+    regenerated arrays must equal the fixture's, so the solve runs on the very
+    bytes the reference solved."""
+    import hashlib
+    import json
+    from amfls_solver_gb300 import problems
+
+    data = dict(np.load(GOLDEN / f"{name}.npz"))
+    spec = json.loads(str(data["generator"]))
+    prob = problems.FAMILIES[spec["family"]](**spec["kwargs"])
+    h = hashlib.sha256()
+    if hasattr(prob, "row_offsets"):
+        parts = (prob.row_offsets, prob.column_indices, prob.values, prob.b)
+    else:
+        parts = (prob.matrix, prob.b)
+    for a in parts:
+        h.update(np.ascontiguousarray(a).tobytes(order="A"))
+    assert h.hexdigest() == str(data["digest"]), f"{name}: regenerated problem differs"
+    return data, prob
+
+
 SOLVE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("solve_*.npz"))
+REPLAY_FIXTURES = sorted(p.stem for p in GOLDEN.glob("replay_*.npz"))
 BASELINE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("baseline_*.npz"))
 
 

@@ -12,9 +12,20 @@ without the reference read them as plain data.
 Only deterministic runs are stored: CSR operators never widen under the
 reference's default cost model, and fixed-width RBGK has no width controller.
 AMFLS widening on dense operators depends on measured seconds and is not
-reproducible across machines, so dense AMFLS fixtures use cases whose
-outcome does not depend on timing (basis-limited ridge, maximum_epochs=0 with
-auxiliary width 0, or a depth cap of one level).
+reproducible across machines, so the plain dense AMFLS fixtures use cases
+whose outcome does not depend on timing (basis-limited ridge,
+maximum_epochs=0 with auxiliary width 0, or a depth cap of one level).
+
+Widening solves are stored as schedule-replay fixtures (``replay``): the
+reference build records the candidate bit of every width decision
+(oracle/ref_hooks.hpp wraps amfls.cpp:323-354); the fixture keeps that list,
+and the reference run *replaying* it (which reproduces the recorded run
+exactly, checked here) gives the stored outputs.  A solver that takes the
+same bits follows the same widening path whatever its own timings.  Large
+inputs (the 20000 x 5000 CSR workload, 16384 x 512 dense matrices) are not
+stored: the fixture names the seeded generator in amfls_solver_gb300.problems
+and the SHA-256 of the generated arrays, so a test regenerates them and
+checks that it has the same bytes.
 """
 from __future__ import annotations
 
@@ -73,6 +84,77 @@ def solve_fixture(name, p, arrays, **opts):
     c = r["counters"]
     print(f"   status {r['status']}/{r['stop_reason']} depth {c[9]} aux {c[10]} "
           f"basis {c[11]} evals {len(r['trace_int'])} disp {c[35]}")
+
+
+def problem_digest(p):
+    """SHA-256 of a generated problem's arrays (CSR or dense) and b."""
+    import hashlib
+    h = hashlib.sha256()
+    if hasattr(p, "row_offsets"):
+        parts = (p.row_offsets, p.column_indices, p.values, p.b)
+    else:
+        parts = (np.asfortranarray(p.matrix) if not p.matrix.flags.c_contiguous
+                 else p.matrix, p.b)
+    for a in parts:
+        h.update(np.ascontiguousarray(a).tobytes(order="A"))
+    return h.hexdigest()
+
+
+def replay_fixture(name, generator, **opts):
+    """A solve on a regenerated problem: `generator` = (family, kwargs) of
+    amfls_solver_gb300.problems (kwargs include the seed).  The reference runs
+    once with its own timing-driven controller; its decision bits are then
+    replayed by the reference (or `opts["replay"]` is replayed directly), and
+    that replayed run must reproduce itself exactly before it is stored."""
+    import json
+    family, kwargs = generator
+    p = problems.FAMILIES[family](**kwargs)
+    replay = opts.pop("replay", None)
+    if replay is None:
+        first = ref.solve(p, **opts)
+        replay = [int(v) for v in first["decisions"]]
+    r = ref.solve(p, replay=replay, **opts)
+    again = ref.solve(p, replay=replay, **opts)
+    if not (np.array_equal(r["counters"][:35], again["counters"][:35]) and
+            np.array_equal(r["solution"], again["solution"]) and r["replay_overrun"] == 0):
+        raise RuntimeError(f"{name}: the replayed reference run is not reproducible")
+    options = np.array([opts.get("regularization", 0.0), opts.get("tolerance", 1e-8),
+                        opts.get("failure_probability", 1e-6)])
+    ints = np.array([opts.get("maximum_epochs", 0), opts.get("maximum_depth", 0),
+                     opts.get("maximum_auxiliary_width", 0), opts.get("maximum_basis_size", 0),
+                     opts.get("seed", 0), opts.get("stream", 0), 4, 0], dtype=np.int64)
+    save(name, generator=np.array(json.dumps({"family": family, "kwargs": kwargs})),
+         digest=np.array(problem_digest(p)), options=options, int_options=ints,
+         replay=np.array(replay, dtype=np.int32), decisions=r["decisions"],
+         solution=r["solution"], metrics=r["metrics"], counters=r["counters"],
+         trace_float=r["trace_float"], trace_int=r["trace_int"],
+         status=np.int64(r["status"]), stop_reason=np.int64(r["stop_reason"]))
+    c = r["counters"]
+    print(f"   status {r['status']}/{r['stop_reason']} depth {c[9]} aux {c[10]} basis {c[11]} "
+          f"widenings {c[34]} decisions {''.join(map(str, r['decisions']))}")
+
+
+def replays():
+    """The 20000 x 5000 CSR workload (bench seed) and widening solves."""
+    replay_fixture("replay_csr_20000x5000",
+                   ("scaled_uniform_csr", dict(m=20000, n=5000, per_row=10, decades=6.0,
+                                               noise=1e-8, seed=20251203)),
+                   regularization=0.0, tolerance=1e-8)
+    # dense column-major operators on which the reference's own cost gate widens
+    replay_fixture("replay_dense_widening_16384x512",
+                   ("scaled_dense", dict(m=16384, n=512, decades=6.0, seed=7, column_major=True)),
+                   regularization=0.0, tolerance=1e-10, seed=3)
+    replay_fixture("replay_dense_widening_8000x400",
+                   ("scaled_dense", dict(m=8000, n=400, decades=6.0, seed=7, column_major=True)),
+                   regularization=0.0, tolerance=1e-10, seed=3)
+    # forced widening schedules on CSR operators (the reference's cost model never
+    # widens there): ridge widened at every decision site, least squares at three
+    replay_fixture("replay_csr_ridge_forced",
+                   ("scaled_uniform_csr", dict(m=2000, n=500, seed=1)),
+                   regularization=1e-4, tolerance=1e-10, seed=7, replay=[1] * 64)
+    replay_fixture("replay_csr_ls_forced",
+                   ("scaled_uniform_csr", dict(m=2000, n=500, seed=1)),
+                   regularization=0.0, tolerance=1e-8, seed=7, replay=[0, 1, 1, 0, 1] + [0] * 64)
 
 
 def main():
@@ -192,9 +274,13 @@ def baselines():
 
 
 if __name__ == "__main__":
-    # no argument: every fixture; "baselines": only the LSQR / LSMR ones
+    # no argument: every fixture; "baselines": only the LSQR / LSMR ones;
+    # "replays": only the schedule-replay fixtures
     if sys.argv[1:] == ["baselines"]:
         baselines()
+    elif sys.argv[1:] == ["replays"]:
+        replays()
     else:
         main()
         baselines()
+        replays()

@@ -1,0 +1,122 @@
+"""The CUDA solve in schedule-replay mode against the reference's widening
+solves and the 20000 x 5000 CSR workload.
+
+The reference's width controller weighs measured seconds, so on its own the
+GPU takes other widening decisions than the CPU reference.  Replaying the
+reference's recorded candidate bits (amfls_gpu_solve_amfls_replay; the bits
+are the only timing-dependent part of a decision, amfls.cpp:323-354) must
+make the GPU take the same decisions at the same sites and so reproduce the
+reference's widening path: identical status, stop reason, depth, auxiliary
+width, basis rank, iterations, operator and search column counts, Gaussian
+seed counts, per-checkpoint status / stop reason / success and the
+per-checkpoint work columns of the trace.
+
+x is fixed only to about cond(A) * tol by the backward-error test; the checks
+on x are the host-recomputed certificate (backward error for lambda = 0,
+relative energy error against an exact dense ridge solution for lambda > 0)
+at most tol, and x within 1e-4 relative of the reference's x (the spread of
+x between the reference and an exact dense least-squares solve on the
+20000 x 5000 problem is 1.1e-4).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import REPLAY_FIXTURES, golden_options, load_replay
+
+pytestmark = pytest.mark.gpu
+
+# counters compared exactly: a/at columns and calls, search columns, iterations,
+# depth, auxiliary width, basis rank, Gaussian columns / values / requests
+EXACT_COUNTERS = [0, 1, 2, 3, 4, 5, 8, 9, 10, 11, 20, 21, 34]
+
+
+@pytest.fixture(scope="module")
+def amfls():
+    import amfls_solver_gb300 as m
+
+    m.load_library()
+    return m
+
+
+def _device_matrix(prob):
+    if hasattr(prob, "row_offsets"):
+        return torch.sparse_csr_tensor(torch.from_numpy(prob.row_offsets),
+                                       torch.from_numpy(prob.column_indices),
+                                       torch.from_numpy(prob.values),
+                                       size=(prob.rows, prob.cols)).cuda()
+    mat = prob.matrix
+    if mat.flags.c_contiguous:
+        return torch.from_numpy(mat).cuda()
+    return torch.from_numpy(np.ascontiguousarray(mat.T)).cuda().t()
+
+
+def _host_certificate(prob, x, reg):
+    """Backward error (lambda = 0) or relative energy error against the exact
+    ridge solution (lambda > 0), in float64 on the host; the operator norm is
+    the largest singular value (dense) or a converged power-iteration estimate
+    (CSR), a lower estimate, so the certificate is not understated."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+
+    if hasattr(prob, "row_offsets"):
+        a = sp.csr_matrix((prob.values, prob.column_indices, prob.row_offsets),
+                          shape=(prob.rows, prob.cols))
+        norm_a = spl.svds(a, k=1, return_singular_vectors=False, tol=1e-10)[0]
+    else:
+        a = np.asarray(prob.matrix)
+        norm_a = np.linalg.norm(a, 2)
+    b = prob.b
+    if reg == 0.0:
+        r = a @ x - b
+        compat = np.linalg.norm(r) / (norm_a * np.linalg.norm(x) + np.linalg.norm(b))
+        ls = np.linalg.norm(a.T @ r) / (norm_a * np.linalg.norm(r))
+        return min(compat, ls)
+    ad = a.toarray() if hasattr(a, "toarray") else a
+    aug = np.vstack([ad, np.sqrt(reg) * np.eye(ad.shape[1])])
+    xl = np.linalg.lstsq(aug, np.concatenate([b, np.zeros(ad.shape[1])]), rcond=None)[0]
+    hnorm = lambda v: np.sqrt(np.linalg.norm(ad @ v) ** 2 + reg * np.linalg.norm(v) ** 2)
+    return hnorm(x - xl) / hnorm(x)
+
+
+@pytest.mark.parametrize("name", REPLAY_FIXTURES)
+def test_gpu_replays_reference(amfls, name):
+    data, prob = load_replay(name)
+    opts = golden_options(data)
+    op = amfls.DeviceOperator(_device_matrix(prob))
+    b = torch.from_numpy(prob.b).cuda()
+    r, decisions, overrun = amfls.solve_amfls_replay(op, b, [int(v) for v in data["replay"]],
+                                                     **opts)
+    assert overrun == 0
+    np.testing.assert_array_equal(decisions, data["decisions"])
+    assert (r.status, r.stop_reason) == (int(data["status"]), int(data["stop_reason"]))
+    c = data["counters"]
+    counters = [r.a_columns, r.at_columns, r.a_block_calls, r.at_block_calls,
+                r.search_a_columns, r.search_at_columns, r.iterations, r.depth,
+                r.auxiliary_width, r.basis_rank, r.gaussian_random_columns,
+                r.gaussian_random_values, r.gaussian_random_block_requests]
+    assert counters == [int(c[i]) for i in EXACT_COUNTERS]
+    assert r.trace_int.shape == data["trace_int"].shape
+    np.testing.assert_array_equal(r.trace_int[:, :3].numpy(), data["trace_int"][:, :3])
+    np.testing.assert_array_equal(r.trace_float[:, :8].numpy(), data["trace_float"][:, :8])
+    reg, tol = opts["regularization"], opts["tolerance"]
+    x, xr = r.solution.cpu().numpy(), data["solution"]
+    if r.status == 0:
+        cert = r.relative_energy_error_upper_bound if reg > 0 else r.backward_error_upper_bound
+        assert cert <= tol
+        assert _host_certificate(prob, x, reg) <= tol * (1 + 1e-3)
+    assert np.linalg.norm(x - xr) <= 1e-4 * np.linalg.norm(xr)
+
+
+def test_gpu_plain_controller_on_csr_workload(amfls):
+    """Without replay the GPU's own controller takes the reference's path on
+    the 20000 x 5000 CSR workload (the reference's CSR cost model never
+    widens): the same counters and trace as the reference's run."""
+    data, prob = load_replay("replay_csr_20000x5000")
+    opts = golden_options(data)
+    r = amfls.run_amfls(_device_matrix(prob), torch.from_numpy(prob.b).cuda(), **opts)
+    c = data["counters"]
+    assert (r.status, r.stop_reason) == (int(data["status"]), int(data["stop_reason"]))
+    assert (r.depth, r.basis_rank, r.auxiliary_width, r.iterations) == (c[9], c[11], c[10], c[8])
+    assert (r.search_a_columns, r.search_at_columns) == (c[4], c[5])
+    np.testing.assert_array_equal(r.trace_int[:, :3].numpy(), data["trace_int"][:, :3])
