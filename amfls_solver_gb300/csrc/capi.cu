@@ -12,6 +12,7 @@
 #include "batch.hpp"
 #include "callback_operator.hpp"
 #include "common.cuh"
+#include "workspace.hpp"
 #include "controller.hpp"
 #include "csr_operator.hpp"
 #include "dense_operator.hpp"
@@ -471,6 +472,14 @@ int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b
         for (int i = 0; i < n; ++i) decisions[i] = sites[i];
         if (decision_count) *decision_count = (int)sites.size();
         if (replay_overrun) *replay_overrun = overrun;
+    });
+}
+
+int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream,
+                                        double* seconds) {
+    return guarded([&] {
+        if (seconds == nullptr) throw std::invalid_argument("seconds must not be null");
+        amfls_gpu::probe_reorthogonalization(n, k, reps, as_stream(stream), seconds);
     });
 }
 

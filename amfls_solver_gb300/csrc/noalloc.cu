@@ -38,11 +38,15 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocScratchDouble
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch_ptr[kMaxDevices] = {};
+int g_sm_count[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device.  Looked up once
-// per device (with that device current) and cached; the name of the array
-// in host code is only a host-side stand-in, not a device address.
-double* scratch_on_current_device() {
+// Device address of the scratch array on the current device, and that
+// device's SM count (for the launch sizes).  Looked up once per device (with
+// that device current) and cached for the life of the process: the name of
+// the array in host code is only a host-side stand-in, not a device address.
+// The cached address belongs to the device's primary context; a
+// cudaDeviceReset (or any other teardown of that context) invalidates it.
+double* scratch_on_current_device(int* sm_count) {
     int dev = -1;
     AMFLS_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("device ordinal out of range");
@@ -50,8 +54,12 @@ double* scratch_on_current_device() {
     if (g_scratch_ptr[dev] == nullptr) {
         void* ptr = nullptr;
         AMFLS_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_partials));
+        int sms = 0;
+        AMFLS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        g_sm_count[dev] = std::max(1, sms);
         g_scratch_ptr[dev] = static_cast<double*>(ptr);
     }
+    *sm_count = g_sm_count[dev];
     return g_scratch_ptr[dev];
 }
 
@@ -94,10 +102,13 @@ extern "C" int amfls_gpu_dense_apply_transpose_noalloc(int rows, int cols, const
                 "dense no-alloc transpose product: cols = " + std::to_string(cols) +
                 " exceeds the fixed scratch of " + std::to_string(kNoAllocScratchDoubles) +
                 " doubles; use amfls_gpu_operator_apply_transpose instead");
-        double* scratch = scratch_on_current_device();
-        // as many row chunks as fill the GPU, bounded by the scratch capacity
+        int sms = 1;
+        double* scratch = scratch_on_current_device(&sms);
+        // as many row chunks as fill the GPU (8 blocks per SM), bounded by the
+        // scratch capacity
         const int col_blocks = (cols + 255) / 256;
-        long long chunks = std::max(1, std::min((152 * 8 + col_blocks - 1) / col_blocks,
+        const int target_blocks = 8 * sms;
+        long long chunks = std::max(1, std::min((target_blocks + col_blocks - 1) / col_blocks,
                                                 (rows + 63) / 64));
         chunks = std::min<long long>(chunks, kNoAllocScratchDoubles / cols);
         const int chunk = static_cast<int>((rows + chunks - 1) / chunks);
@@ -106,7 +117,7 @@ extern "C" int amfls_gpu_dense_apply_transpose_noalloc(int rows, int cols, const
         noalloc_chunk_sums<<<dim3(col_blocks, static_cast<unsigned>(chunks)), 256, 0, s>>>(
             d_values, rows, cols, chunk, d_y, scratch);
         AMFLS_LAUNCHED();
-        noalloc_add_chunks<<<std::max(1, std::min(col_blocks, 1216)), 256, 0, s>>>(
+        noalloc_add_chunks<<<std::max(1, std::min(col_blocks, target_blocks)), 256, 0, s>>>(
             scratch, static_cast<int>(chunks), cols, d_x);
         AMFLS_LAUNCHED();
         set_last_error("");

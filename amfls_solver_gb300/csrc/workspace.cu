@@ -969,4 +969,94 @@ void Workspace::solve_projected(double* d_x) {
     projected_flags_ = (int)st[5];
 }
 
+namespace {
+
+__global__ void probe_fill_kernel(double* const* panels, int n, int k, double* r) {
+    const long long total = (long long)n * 32;
+    const int P = (k + 31) / 32;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total * P;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(i / total);
+        const long long e = i - (long long)p * total;
+        const long long row = e / 32;
+        const int col = p * 32 + (int)(e % 32);
+        panels[p][e] = col < k ? (double)((row * 7 + col * 13) % 17 - 8) * 1e-3 : 0.0;
+        if (p == 0 && e % 32 == 0) r[row] = (double)((row * 5) % 11 - 5) * 1e-2;
+    }
+}
+
+}  // namespace
+
+void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double seconds[2]) {
+    if (n <= 0 || k <= 0 || reps <= 0) throw std::invalid_argument("probe sizes must be positive");
+    const int P = (k + 31) / 32;
+    int pcap = 4;
+    while (pcap < P) pcap *= 2;
+    PanelStore V(n, pcap, s);
+    V.ensure_columns(k);
+    double *r = nullptr, *w = nullptr, *c = nullptr, *partials = nullptr;
+    unsigned* counters = nullptr;
+    DevState* st = nullptr;
+    const long long vc_off = (long long)(kGemvTargetBlocks + pcap) * 32 + 6 * 1216;
+    stream_alloc(&r, sizeof(double) * n, s);
+    stream_alloc(&w, sizeof(double) * n, s);
+    stream_alloc(&c, sizeof(double) * 32 * pcap, s);
+    stream_alloc(&partials, sizeof(double) * (vc_off + (n + 31) / 32 + 1024), s);
+    stream_alloc(&counters, sizeof(unsigned) * (64 + pcap + 64), s);
+    stream_alloc(&st, sizeof(DevState), s);
+    AMFLS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned) * (64 + pcap + 64), s));
+    DevState h;
+    std::memset(&h, 0, sizeof(h));
+    h.k = k;
+    h.go = 1;
+    h.reliable = 1;
+    h.basis_limit = k + 1;
+    h.right_scale = 1.0;
+    h.norm_before = 1e300;  // the pass never decides the level: state stays as set
+    AMFLS_CUDA(cudaMemcpyAsync(st, &h, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    probe_fill_kernel<<<1216, 256, 0, s>>>(V.device_table(), n, k, r);
+    AMFLS_LAUNCHED();
+    const int max_chunks = (int)std::max<long long>(1, (n + 255) / 256);
+    const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + pcap - 1) / pcap));
+    const int chunk_rows = (int)(((long long)n + chunks - 1) / chunks);
+    const dim3 tgrid(pcap, chunks);
+    const int ngrid = (int)((n + 31) / 32);
+    auto vt = [&] {
+        vt_r_kernel<<<tgrid, kThreads, 0, s>>>(V.device_table(), n, chunk_rows, r, c, partials,
+                                               counters + 64, st, 1);
+        AMFLS_LAUNCHED();
+    };
+    auto vc = [&] {
+        v_c_kernel<<<ngrid, kThreads, 0, s>>>(V.device_table(), n, -1, c, r, w, 0,
+                                              partials + vc_off, counters + 3, st,
+                                              kHookRightPass1, n, 1, 1);
+        AMFLS_LAUNCHED();
+    };
+    cudaEvent_t e[3];
+    for (auto& ev : e) AMFLS_CUDA(cudaEventCreate(&ev));
+    for (int i = 0; i < 3; ++i) {  // warm-up
+        vt();
+        vc();
+    }
+    AMFLS_CUDA(cudaEventRecord(e[0], s));
+    for (int i = 0; i < reps; ++i) vt();
+    AMFLS_CUDA(cudaEventRecord(e[1], s));
+    for (int i = 0; i < reps; ++i) vc();
+    AMFLS_CUDA(cudaEventRecord(e[2], s));
+    AMFLS_CUDA(cudaEventSynchronize(e[2]));
+    float ms0 = 0.f, ms1 = 0.f;
+    AMFLS_CUDA(cudaEventElapsedTime(&ms0, e[0], e[1]));
+    AMFLS_CUDA(cudaEventElapsedTime(&ms1, e[1], e[2]));
+    for (auto& ev : e) cudaEventDestroy(ev);
+    seconds[0] = ms0 * 1e-3 / reps;
+    seconds[1] = ms1 * 1e-3 / reps;
+    stream_free(r, s);
+    stream_free(w, s);
+    stream_free(c, s);
+    stream_free(partials, s);
+    stream_free(counters, s);
+    stream_free(st, s);
+    stream_wait(s);
+}
+
 }  // namespace amfls_gpu

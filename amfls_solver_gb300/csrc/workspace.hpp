@@ -232,4 +232,11 @@ private:
     cudaEvent_t ev_[2] = {nullptr, nullptr};
 };
 
+// Times the width-one reorthogonalisation sweeps (c = V^T r and the
+// r -> r - V c pass with its norm and DGKS test, krylov_workspace.cpp:152-165)
+// exactly as a level launches them, on a basis of n rows and k columns in the
+// panel layout filled with a fixed pattern: `reps` launches of each, CUDA
+// events on `stream`; seconds[0] / seconds[1] receive the mean per launch.
+void probe_reorthogonalization(int n, int k, int reps, cudaStream_t stream, double seconds[2]);
+
 }  // namespace amfls_gpu

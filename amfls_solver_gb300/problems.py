@@ -22,6 +22,9 @@ Families
     (the 4Mx1M learned-width family).
 ``scaled_dense``  G diag(d) with G i.i.d. N(0,1), d geometric from 1 to
     10^-decades, b ~ N(0,1) (the 100000x2000 dense workload).
+``portable_dense`` / ``portable_csr``  the same shapes from integer draws
+    and power-of-two scalings only: bit-identical on every platform (the
+    families above call libm, whose last bits differ between machines).
 """
 from __future__ import annotations
 
@@ -166,6 +169,53 @@ def scaled_dense(m: int, n: int, decades: float = 6.0, seed: int = 0,
     return DenseProblem(g, b)
 
 
+def portable_dense(m: int, n: int, octaves: int = 20, seed: int = 0,
+                   column_major: bool = True) -> DenseProblem:
+    """G diag(d) built from integer draws only: G_ij = k_ij 2^-20 with k_ij
+    uniform in [-2^20, 2^20], d_j = 2^-floor(octaves j / (n - 1)) (condition
+    about 2^octaves), b_i = k_i 2^-20.  Integer streams of a seeded numpy
+    Generator and exact power-of-two scalings involve no libm call, so the
+    arrays are the same bytes on every platform (the generators above use
+    exp / log / pow, whose last bits differ between x86-64 and AArch64)."""
+    rng = np.random.default_rng(seed)
+    lim = 1 << 20
+    shape = (n, m) if column_major else (m, n)
+    g = np.ldexp(rng.integers(-lim, lim, size=shape, endpoint=True).astype(np.float64), -20)
+    if column_major:
+        g = np.asfortranarray(g.T)
+    d = np.ldexp(1.0, -((octaves * np.arange(n)) // max(1, n - 1)))
+    g *= d[None, :]
+    b = np.ldexp(rng.integers(-lim, lim, size=m, endpoint=True).astype(np.float64), -20)
+    return DenseProblem(g, b)
+
+
+def portable_csr(m: int, n: int, per_row: int = 10, octaves: int = 20, noise_bits: int = 27,
+                 seed: int = 0) -> CsrProblem:
+    """CSR counterpart of portable_dense: per_row distinct uniform columns per
+    row, values k 2^-20 scaled by 2^-floor(octaves j / n), b = A x_true plus
+    integer noise of 2^-noise_bits units, x_true_j = k_j 2^-20.  The same
+    bytes on every platform (b's sums are IEEE additions in a fixed order)."""
+    rng = np.random.default_rng(seed)
+    lim = 1 << 20
+    lengths = np.full(m, min(per_row, n), dtype=np.int64)
+    cols = _distinct_columns(rng, lengths, n)
+    offsets = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(lengths, out=offsets[1:])
+    values = np.ldexp(rng.integers(-lim, lim, size=cols.shape[0], endpoint=True)
+                      .astype(np.float64), -20)
+    values *= np.ldexp(1.0, -((octaves * cols) // n))
+    prob = CsrProblem(m, n, offsets, cols, values, np.zeros(m))
+    x_true = np.ldexp(rng.integers(-lim, lim, size=n, endpoint=True).astype(np.float64), -20)
+    row_ids = np.repeat(np.arange(m), lengths)
+    b = np.zeros(m)
+    np.add.at(b, row_ids, values * x_true[cols])  # sequential per element: fixed order
+    b += np.ldexp(rng.integers(-lim, lim, size=m, endpoint=True).astype(np.float64),
+                  -20 - noise_bits)
+    prob.b = b
+    prob.x_true = x_true
+    return prob
+
+
 def uneven_csr_batch(count: int = 256, seed: int = 0, m_range=(2_000, 200_000),
                      n_range=(500, 50_000), per_row=(5, 40), cond_range=(1e3, 1e8),
                      reg_range=(1e-8, 1e-2), tolerance: float = 1e-9, noise: float = 1e-8):
@@ -211,6 +261,8 @@ WORKLOADS = {
 }
 
 FAMILIES = {
+    "portable_dense": portable_dense,
+    "portable_csr": portable_csr,
     "scaled_uniform_csr": scaled_uniform_csr,
     "power_law_csr": power_law_csr,
     "banded_random_csr": banded_random_csr,

@@ -297,6 +297,16 @@ int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b
                                  double* trace_float, int64_t* trace_int, int trace_capacity,
                                  void* stream);
 
+/* Measurement hook (no counterpart in the reference): times the two
+ * width-one reorthogonalisation sweeps of a level (c = V^T r, then
+ * r -> r - V c with its norm and DGKS test; krylov_workspace.cpp:152-165) on
+ * a basis of n rows and k columns in the solver's own layout, filled with a
+ * fixed pattern: `reps` launches of each after a warm-up, CUDA events on
+ * `stream`.  seconds[0] and seconds[1] receive the mean seconds per launch of
+ * the V^T r and the V c sweep.  Allocates 8 n k bytes for the duration of
+ * the call; synchronous. */
+int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream, double* seconds);
+
 /* Batched AMFLS (no counterpart in the reference): `count` independent
  * problems, problem i = (ops[i], d_b[i], options[i]) with its solution in
  * d_solutions[i] (a distinct operator per problem: an operator's products
@@ -321,7 +331,10 @@ int amfls_gpu_solve_amfls_batch(int count, const amfls_gpu_operator* const* ops,
  * library holds until exit; cols above that capacity are rejected with
  * AMFLS_GPU_LENGTH_ERROR.  The first call on each device looks the array's
  * device address up (cudaGetSymbolAddress) with that device current, so make
- * that first call before any stream capture.  All calls share the array:
+ * that first call before any stream capture.  The address is cached for the
+ * life of the device's primary context: after cudaDeviceReset (or another
+ * teardown of that context) do not call this entry point again in the
+ * process.  All calls share the array:
  * calls whose kernels may overlap on the GPU (unordered streams) race; calls
  * ordered on one stream are safe.  Asynchronous on `stream`. */
 int amfls_gpu_dense_apply_transpose_noalloc(int rows, int cols, const double* d_values,

@@ -48,17 +48,23 @@ def golden_options(data):
 
 
 def load_replay(name):
-    """A schedule-replay fixture and its regenerated problem.  The problem is
-    rebuilt from the seeded generator the fixture names; the SHA-256 of the
-    regenerated arrays must equal the fixture's, so the solve runs on the very
+    """A schedule-replay fixture and its problem: the arrays stored in the
+    fixture, or else the problem rebuilt from the seeded generator it names
+    (the portable families, bit-identical on every platform).  The SHA-256
+    of the arrays must equal the fixture's, so the solve runs on the very
     bytes the reference solved."""
     import hashlib
     import json
     from amfls_solver_gb300 import problems
 
     data = dict(np.load(GOLDEN / f"{name}.npz"))
-    spec = json.loads(str(data["generator"]))
-    prob = problems.FAMILIES[spec["family"]](**spec["kwargs"])
+    if "row_offsets" in data:  # stored arrays (the generator calls libm)
+        prob = problems.CsrProblem(int(data["rows"]), int(data["cols"]), data["row_offsets"],
+                                   data["column_indices"].astype(np.int64), data["values"],
+                                   data["b"])
+    else:
+        spec = json.loads(str(data["generator"]))
+        prob = problems.FAMILIES[spec["family"]](**spec["kwargs"])
     h = hashlib.sha256()
     if hasattr(prob, "row_offsets"):
         parts = (prob.row_offsets, prob.column_indices, prob.values, prob.b)

@@ -100,12 +100,15 @@ def problem_digest(p):
     return h.hexdigest()
 
 
-def replay_fixture(name, generator, **opts):
+def replay_fixture(name, generator, store=False, **opts):
     """A solve on a regenerated problem: `generator` = (family, kwargs) of
     amfls_solver_gb300.problems (kwargs include the seed).  The reference runs
     once with its own timing-driven controller; its decision bits are then
     replayed by the reference (or `opts["replay"]` is replayed directly), and
-    that replayed run must reproduce itself exactly before it is stored."""
+    that replayed run must reproduce itself exactly before it is stored.
+    store=True keeps the CSR arrays in the fixture (for generators that call
+    libm, whose results differ in the last bits between platforms); the
+    portable_* families regenerate bit for bit anywhere."""
     import json
     family, kwargs = generator
     p = problems.FAMILIES[family](**kwargs)
@@ -123,37 +126,47 @@ def replay_fixture(name, generator, **opts):
     ints = np.array([opts.get("maximum_epochs", 0), opts.get("maximum_depth", 0),
                      opts.get("maximum_auxiliary_width", 0), opts.get("maximum_basis_size", 0),
                      opts.get("seed", 0), opts.get("stream", 0), 4, 0], dtype=np.int64)
+    stored = {}
+    if store:
+        stored = dict(rows=np.int64(p.rows), cols=np.int64(p.cols), row_offsets=p.row_offsets,
+                      column_indices=p.column_indices.astype(np.int32), values=p.values, b=p.b)
     save(name, generator=np.array(json.dumps({"family": family, "kwargs": kwargs})),
          digest=np.array(problem_digest(p)), options=options, int_options=ints,
          replay=np.array(replay, dtype=np.int32), decisions=r["decisions"],
          solution=r["solution"], metrics=r["metrics"], counters=r["counters"],
          trace_float=r["trace_float"], trace_int=r["trace_int"],
-         status=np.int64(r["status"]), stop_reason=np.int64(r["stop_reason"]))
+         status=np.int64(r["status"]), stop_reason=np.int64(r["stop_reason"]), **stored)
     c = r["counters"]
     print(f"   status {r['status']}/{r['stop_reason']} depth {c[9]} aux {c[10]} basis {c[11]} "
           f"widenings {c[34]} decisions {''.join(map(str, r['decisions']))}")
 
 
 def replays():
-    """The 20000 x 5000 CSR workload (bench seed) and widening solves."""
+    """The 20000 x 5000 CSR workload (bench seed; arrays stored) and widening
+    solves on portable problems."""
     replay_fixture("replay_csr_20000x5000",
                    ("scaled_uniform_csr", dict(m=20000, n=5000, per_row=10, decades=6.0,
                                                noise=1e-8, seed=20251203)),
-                   regularization=0.0, tolerance=1e-8)
-    # dense column-major operators on which the reference's own cost gate widens
+                   store=True, regularization=0.0, tolerance=1e-8)
+    # dense column-major operators on which the reference's own cost gate
+    # widens (its decisions vary from run to run with the measured seconds;
+    # the fixture keeps the run it recorded)
     replay_fixture("replay_dense_widening_16384x512",
-                   ("scaled_dense", dict(m=16384, n=512, decades=6.0, seed=7, column_major=True)),
+                   ("portable_dense", dict(m=16384, n=512, octaves=20, seed=7)),
                    regularization=0.0, tolerance=1e-10, seed=3)
-    replay_fixture("replay_dense_widening_8000x400",
-                   ("scaled_dense", dict(m=8000, n=400, decades=6.0, seed=7, column_major=True)),
+    replay_fixture("replay_dense_widening_8192x400",
+                   ("portable_dense", dict(m=8192, n=400, octaves=20, seed=7)),
+                   regularization=0.0, tolerance=1e-10, seed=3)
+    replay_fixture("replay_dense_widening_2500x200",
+                   ("portable_dense", dict(m=2500, n=200, octaves=20, seed=1)),
                    regularization=0.0, tolerance=1e-10, seed=3)
     # forced widening schedules on CSR operators (the reference's cost model never
     # widens there): ridge widened at every decision site, least squares at three
     replay_fixture("replay_csr_ridge_forced",
-                   ("scaled_uniform_csr", dict(m=2000, n=500, seed=1)),
+                   ("portable_csr", dict(m=2000, n=500, seed=1)),
                    regularization=1e-4, tolerance=1e-10, seed=7, replay=[1] * 64)
     replay_fixture("replay_csr_ls_forced",
-                   ("scaled_uniform_csr", dict(m=2000, n=500, seed=1)),
+                   ("portable_csr", dict(m=2000, n=500, seed=1)),
                    regularization=0.0, tolerance=1e-8, seed=7, replay=[0, 1, 1, 0, 1] + [0] * 64)
 
 

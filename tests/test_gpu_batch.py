@@ -32,6 +32,29 @@ def test_batch_matches_one_at_a_time():
             assert hn(r.solution - one.solution) <= 10 * tol * 1e5 * hn(one.solution)
 
 
+def test_batch_matches_oracle():
+    """Batched CSR solves against the oracle (the CPU restatement pinned to
+    the reference): CSR operators never widen under the reference's cost
+    model, so each problem's status, stop reason, depth and basis rank must
+    equal the oracle's solve of it, and the certified bound must meet tol."""
+    import amfls_solver_gb300 as amfls
+    from amfls_solver_gb300 import problems
+    from oracle import amfls_oracle as orc
+
+    batch = problems.uneven_csr_batch(6, seed=9, m_range=(2000, 8000), n_range=(500, 2000),
+                                      cond_range=(1e3, 1e5))
+    mats = [(csr_tensor(p), torch.from_numpy(p.b).cuda()) for p, _, _ in batch]
+    regs = [r for _, r, _ in batch]
+    tol = batch[0][2]
+    results, _, _ = amfls.run_amfls_batch(mats, workers=3, regularization=regs, tolerance=tol)
+    for (p, reg, _), r in zip(batch, results):
+        ref = orc.solve_amfls(p, regularization=reg, tolerance=tol)
+        assert (r.status, r.stop_reason) == (ref["status"], ref["stop_reason"])
+        assert (r.depth, r.basis_rank) == (int(ref["counters"][9]), int(ref["counters"][11]))
+        if r.status == 0:
+            assert r.relative_energy_error_upper_bound <= tol
+
+
 def test_batch_reports_bad_problems_without_stopping_the_others():
     import amfls_solver_gb300 as amfls
     from amfls_solver_gb300 import problems

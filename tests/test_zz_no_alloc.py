@@ -6,9 +6,9 @@ the device, under a host memory manager that owns all device memory).  It
 keeps its partial sums in a fixed device array shared by all calls, so this
 test runs it twice in a row (the second call sees the first call's leftover
 partials) and compares both results with the regular entry point,
-amfls_gpu_operator_apply_transpose on a dense operator, to the product's
-rounding model.  This file sorts last so a stop-at-first-failure run has
-already run every other test.
+amfls_gpu_operator_apply_transpose on a dense operator, and with a float64
+numpy product A^T y, to the product's rounding model.  This file sorts last
+so a stop-at-first-failure run has already run every other test.
 """
 import ctypes
 
@@ -40,20 +40,21 @@ def noalloc_transpose(lib, a, y):
 def test_noalloc_matches_regular_entry_point_twice(native):
     amfls, lib = native
     rng = np.random.default_rng(7)
-    a = torch.from_numpy(rng.standard_normal((3000, 700))).cuda()
+    a_host = rng.standard_normal((3000, 700))
+    a = torch.from_numpy(a_host).cuda()
     op = amfls.DeviceOperator(a)
-    abs_a = a.abs()
     for seed in (1, 2):  # two calls in a row share the scratch array
-        y = torch.from_numpy(np.random.default_rng(seed).standard_normal(3000)).cuda()
-        ref = op.apply(y, transpose=True)
-        got = noalloc_transpose(lib, a, y)
-        torch.cuda.synchronize()
+        y_host = np.random.default_rng(seed).standard_normal(3000)
+        y = torch.from_numpy(y_host).cuda()
+        ref = op.apply(y, transpose=True).cpu().numpy()
+        got = noalloc_transpose(lib, a, y).cpu().numpy()
+        exact = a_host.T @ y_host
         # gamma_{2 rows + 2} |A|^T |y|: the reference's rounding model for A^T y
         k = 2 * 3000 + 2
         u = np.finfo(np.float64).eps / 2
-        bound = (abs_a.t() @ y.abs()).cpu().numpy() * (k * u / (1 - k * u))
-        diff = (got - ref).abs().cpu().numpy()
-        assert np.all(diff <= 2 * bound)
+        bound = (np.abs(a_host).T @ np.abs(y_host)) * (k * u / (1 - k * u))
+        assert np.all(np.abs(got - ref) <= 2 * bound)
+        assert np.all(np.abs(got - exact) <= 2 * bound)
 
 
 def test_noalloc_rejects_oversized_input(native):
