@@ -43,7 +43,7 @@ __global__ void scale_kernel(double* v, double f, long long n) {
 }
 
 int grid_for(long long n) {
-    return (int)std::max<long long>(1, std::min<long long>(1216, (n + 255) / 256));
+    return (int)std::max<long long>(1, std::min<long long>(grid_cap(), (n + 255) / 256));
 }
 
 // Device vectors, elementwise kernels, norms and the search-product
@@ -51,7 +51,7 @@ int grid_for(long long n) {
 class Run {
 public:
     Run(const DeviceOperator& op, cudaStream_t s) : op_(op), s_(s) {
-        stream_alloc(&partials_, sizeof(double) * 2 * kMaxVectors * 1216, s_);
+        stream_alloc(&partials_, sizeof(double) * 2 * kMaxVectors * kMaxGridCap, s_);
         stream_alloc(&counter_, sizeof(unsigned), s_);
         stream_alloc(&norms_, sizeof(NormResult), s_);
         AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned), s_));

@@ -652,7 +652,7 @@ block_projected_kernel(const int* __restrict__ meta, const double* __restrict__ 
 }
 
 int ts_chunks(long long m, int tiles) {
-    const long long want = ceil_div(1216, tiles);
+    const long long want = ceil_div(grid_cap(), tiles);
     return static_cast<int>(std::max<long long>(1, std::min<long long>(want, ceil_div(m, 256))));
 }
 
@@ -681,7 +681,7 @@ void ts_tn(const double* X, long long ldx, const double* Y, long long ldy, long 
                                                                   rpc, partials);
     AMFLS_LAUNCHED();
     const long long ab = (long long)a * b;
-    sum_chunks_kernel<<<grid_for(ab, 256, 1216), 256, 0, s>>>(partials, chunks, ab, C, nonfinite);
+    sum_chunks_kernel<<<grid_for(ab, 256, grid_cap()), 256, 0, s>>>(partials, chunks, ab, C, nonfinite);
     AMFLS_LAUNCHED();
 }
 
@@ -691,7 +691,7 @@ void ts_nn(const double* X, long long ldx, const double* C, long long m, int a, 
     const long long ab = (long long)a * b;
     const int in_smem = ab <= 6144 ? 1 : 0;
     const size_t smem = in_smem ? sizeof(double) * std::max<long long>(1, ab) : 0;
-    ts_nn_kernel<<<grid_for(m, kThreads, 1216), kThreads, smem, s>>>(X, ldx, C, m, a, b, Y, ldy,
+    ts_nn_kernel<<<grid_for(m, kThreads, grid_cap()), kThreads, smem, s>>>(X, ldx, C, m, a, b, Y, ldy,
                                                                      alpha, beta, in_smem);
     AMFLS_LAUNCHED();
 }
@@ -712,7 +712,7 @@ void panel_tn(double* const* panels, long long n, int k, const double* R, long l
         panel_tn_partial_kernel<<<dim3(P, chunks), kThreads, 0, s>>>(
             panels, n, R + (long long)c0 * ldr, ldr, cc, rpc, partials);
         AMFLS_LAUNCHED();
-        panel_tn_reduce_kernel<<<grid_for((long long)P * 32 * cc, 256, 1216), 256, 0, s>>>(
+        panel_tn_reduce_kernel<<<grid_for((long long)P * 32 * cc, 256, grid_cap()), 256, 0, s>>>(
             partials, P, chunks, k, cc, C + (long long)c0 * k, k, nonfinite);
         AMFLS_LAUNCHED();
     }

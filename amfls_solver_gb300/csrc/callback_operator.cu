@@ -31,9 +31,9 @@ CallbackOperator::CallbackOperator(int rows, int cols, const Callbacks& cb, cuda
             throw std::invalid_argument("custom operator validation model is invalid");
     }
     AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * (size_t)std::max(rows, cols)));
-    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * 1216 + 64));
+    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxGridCap + 64));
     counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
-                                           sizeof(double) * 6 * 1216);
+                                           sizeof(double) * 6 * kMaxGridCap);
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
 }

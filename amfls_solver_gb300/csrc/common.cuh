@@ -60,6 +60,31 @@ void keep_pool_memory();
 // launch work).
 void stream_wait(cudaStream_t stream);
 
+// Streaming multiprocessors of the current device
+// (cudaDevAttrMultiProcessorCount), queried once per device.
+inline int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    const int slot = dev >= 0 && dev < 64 ? dev : 0;
+    int v = __atomic_load_n(&cached[slot], __ATOMIC_RELAXED);
+    if (v == 0) {
+        check_cuda(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev),
+                   "cudaDeviceGetAttribute(MultiProcessorCount)");
+        v = v > 0 ? v : 1;
+        __atomic_store_n(&cached[slot], v, __ATOMIC_RELAXED);
+    }
+    return v;
+}
+
+// Grid cap of the grid-stride and reduction kernels: eight resident
+// 256-thread blocks per SM.
+inline int grid_cap() { return 8 * sm_count(); }
+
+// Upper bound of grid_cap() (devices of up to 256 SMs), for sizing the
+// per-block partial-sum scratch that is allocated once.
+constexpr int kMaxGridCap = 8 * 256;
+
 constexpr int kWarp = 32;
 constexpr int kPanel = 32;  // columns per V panel (row-major n x 32 tiles)
 

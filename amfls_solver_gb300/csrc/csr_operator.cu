@@ -47,7 +47,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarpsPerBlock = kThreads / 32;
-constexpr int kMaxBlocks = 152 * 8;
+// most CTAs a product launches (eight per SM)
+inline int max_blocks() { return grid_cap(); }
 
 // ------------------------------------------------------------- setup ----
 
@@ -226,11 +227,11 @@ spmv_dd_kernel(const long long* __restrict__ off, const int* __restrict__ idx,
 
 int grid_for(long long warps) {
     long long blocks = (warps + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    return (int)std::max<long long>(1, std::min<long long>(blocks, kMaxBlocks));
+    return (int)std::max<long long>(1, std::min<long long>(blocks, max_blocks()));
 }
 
 int setup_grid(long long items) {
-    return (int)std::max<long long>(1, std::min<long long>((items + 255) / 256, 152 * 16));
+    return (int)std::max<long long>(1, std::min<long long>((items + 255) / 256, 2 * grid_cap()));
 }
 
 }  // namespace
@@ -465,7 +466,7 @@ __global__ void rows_major_kernel(const double* __restrict__ x, long long ld, in
 }
 
 // Resident CTAs for a tile kernel (every warp of the grid walks its own
-// tiles), at most one warp per tile and at most kMaxBlocks CTAs.
+// tiles), at most one warp per tile and at most max_blocks() CTAs.
 template <typename V, int C, int E, bool kFused, bool kChains>
 int tile_grid(int ntiles) {
     // resident CTAs per SM and SM count, set up once per instantiation (a
@@ -482,7 +483,7 @@ int tile_grid(int ntiles) {
         return std::make_pair(std::max(1, nb), sms);
     }();
     const int need = (ntiles + csr_tiles::kWarps - 1) / csr_tiles::kWarps;
-    return std::max(1, std::min({need, occ.first * occ.second, kMaxBlocks}));
+    return std::max(1, std::min({need, occ.first * occ.second, max_blocks()}));
 }
 
 template <int C, bool kFused, bool kChains, typename V>
@@ -617,9 +618,9 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
     Side& T = *t_;
     A.count = rows_;
     T.count = cols_;
-    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kMaxBlocks + 64) + 64));
+    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kMaxGridCap + 64) + 64));
     counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
-                                           sizeof(double) * (6 * kMaxBlocks + 64));
+                                           sizeof(double) * (6 * kMaxGridCap + 64));
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
     AMFLS_CUDA(cudaMalloc(&A.off, sizeof(long long) * (rows_ + 1)));
     AMFLS_CUDA(cudaMalloc(&xrows_, sizeof(double) * 8 * (size_t)std::max(rows_, cols_)));
@@ -899,9 +900,9 @@ ReducedCsrOperator::ReducedCsrOperator(const CsrOperator& src, ValueType type,
             }
         }
         AMFLS_CUDA(cudaMalloc(&xrows_, sizeof(double) * 8 * (size_t)std::max(src.rows_, src.cols_)));
-        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxBlocks + 64));
+        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxGridCap + 64));
         counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
-                                               sizeof(double) * 6 * kMaxBlocks);
+                                               sizeof(double) * 6 * kMaxGridCap);
         AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
         AMFLS_CUDA(cudaStreamSynchronize(stream));
     } catch (...) {

@@ -27,7 +27,8 @@ namespace amfls_gpu {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTargetBlocks = 152 * 8;
+// blocks that fill the GPU (eight per SM)
+inline int target_blocks() { return grid_cap(); }
 
 // ---- block products (s columns per pass over A, s <= 8 per launch) ----
 // Both directions split the long dimension into chunks whose partial sums
@@ -264,7 +265,7 @@ __global__ void epilogue_kernel(const double* __restrict__ t, long long n, Epilo
 }
 
 int grid_1d(long long items) {
-    return (int)std::max<long long>(1, std::min<long long>(kTargetBlocks, (items + 255) / 256));
+    return (int)std::max<long long>(1, std::min<long long>(target_blocks(), (items + 255) / 256));
 }
 
 // chunking for the block kernels: enough blocks to fill the GPU twice over
@@ -276,7 +277,7 @@ void block_chunks(bool dot, int out_n, int in_n, int& blocks_x, int& chunks, int
         blocks_x = (out_n + kThreads - 1) / kThreads;
     }
     const int min_rows = dot ? 256 : 32;
-    chunks = std::max(1, std::min((2 * kTargetBlocks + blocks_x - 1) / blocks_x,
+    chunks = std::max(1, std::min((2 * target_blocks() + blocks_x - 1) / blocks_x,
                                   (in_n + min_rows - 1) / min_rows));
     chunk = (in_n + chunks - 1) / chunks;
     chunks = (in_n + chunk - 1) / chunk;
@@ -316,7 +317,7 @@ DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool co
         throw std::invalid_argument("dense operator input is invalid");
     const int outer = column_major ? cols : rows;
     const int inner = column_major ? rows : cols;
-    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kTargetBlocks + 64)));
+    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kMaxGridCap + 64)));
     AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * 8));
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * 8, stream));
     AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows, cols)));

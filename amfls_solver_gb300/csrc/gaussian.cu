@@ -103,7 +103,7 @@ void project_out_direction(double* R, int rows, int cols, const double* b, doubl
     if (!(bnorm != 0.0) || cols <= 0) return;
     double* dots = nullptr;
     AMFLS_CUDA(cudaMallocAsync(&dots, sizeof(double) * cols, s));
-    direction_dots_kernel<<<std::min(cols, 1216), 256, 0, s>>>(R, rows, cols, b, bnorm, dots);
+    direction_dots_kernel<<<std::min(cols, grid_cap()), 256, 0, s>>>(R, rows, cols, b, bnorm, dots);
     AMFLS_LAUNCHED();
     const long long total = (long long)rows * cols;
     direction_update_kernel<<<(int)std::min<long long>(2432, (total + 255) / 256), 256, 0, s>>>(

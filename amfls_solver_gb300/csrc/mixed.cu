@@ -43,7 +43,7 @@ __global__ void axpy_kernel(const double* a, double s, const double* b, long lon
 }
 
 int grid_for(long long n) {
-    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 8));
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, grid_cap()));
 }
 
 double certificate_of(const ValidationOutput& v, double reg) {

@@ -25,12 +25,13 @@ namespace amfls_gpu {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTargetBlocks = 152 * 8;
+// blocks that fill the GPU (eight per SM)
+inline int target_blocks() { return grid_cap(); }
 constexpr int kMaxCols = 8;  // columns per pass over the matrix
 
 int grid_1d(long long n) {
     return (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads,
-                                                           kTargetBlocks));
+                                                           target_blocks()));
 }
 
 // 16 bytes of T as FP32 values
@@ -181,12 +182,12 @@ Shape shape_of(bool dot, int outer, int inner, int vec) {
     Shape s{};
     if (dot) {
         s.bx = (int)ceil_div(outer, 2 * (kThreads / 32));
-        s.chunks = (int)std::max<long long>(1, std::min<long long>(kTargetBlocks / std::max(1, s.bx),
+        s.chunks = (int)std::max<long long>(1, std::min<long long>(target_blocks() / std::max(1, s.bx),
                                                                    ceil_div(inner, 32LL * vec)));
         s.chunk = (int)(ceil_div(ceil_div(inner, s.chunks), 32LL * vec) * 32 * vec);
     } else {
         s.bx = (int)ceil_div(ceil_div(outer, vec), kThreads);
-        s.chunks = (int)std::max<long long>(1, std::min<long long>(kTargetBlocks / std::max(1, s.bx),
+        s.chunks = (int)std::max<long long>(1, std::min<long long>(target_blocks() / std::max(1, s.bx),
                                                                    inner));
         s.chunk = (int)ceil_div(inner, s.chunks);
     }
@@ -305,9 +306,9 @@ ReducedDenseOperator::ReducedDenseOperator(const DenseOperator& src, ValueType t
         }
         AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * partial_cap_));
         AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows_, cols_)));
-        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kTargetBlocks + 64));
+        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxGridCap + 64));
         counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
-                                               sizeof(double) * 6 * kTargetBlocks);
+                                               sizeof(double) * 6 * kMaxGridCap);
         AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
         AMFLS_CUDA(cudaStreamSynchronize(stream));
     } catch (...) {
@@ -381,9 +382,9 @@ AugmentedOperator::AugmentedOperator(const DeviceOperator& a, double lambda, cud
     try {
         AMFLS_CUDA(cudaMalloc(&top_, sizeof(double) * m * kMaxCols));
         AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * (m + n)));
-        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kTargetBlocks + 64));
+        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxGridCap + 64));
         counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
-                                               sizeof(double) * 6 * kTargetBlocks);
+                                               sizeof(double) * 6 * kMaxGridCap);
         AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
         AMFLS_CUDA(cudaStreamSynchronize(stream));
     } catch (...) {

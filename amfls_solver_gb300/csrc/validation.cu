@@ -585,7 +585,7 @@ __global__ void correction_q_kernel(const double* h, const double* g, const ValS
 }
 
 int vgrid(long long n) {
-    return (int)std::max<long long>(1, std::min<long long>(1216, (n + 255) / 256));
+    return (int)std::max<long long>(1, std::min<long long>(grid_cap(), (n + 255) / 256));
 }
 
 }  // namespace
@@ -617,7 +617,7 @@ struct Validator::Impl {
         alloc(r, m);
         alloc(atr, n);
         alloc(g, n);
-        alloc(partials, 2 * kMaxVectors * 1216 + 8 * 1216);
+        alloc(partials, 2 * kMaxVectors * kMaxGridCap + 8 * kMaxGridCap);
         stream_alloc(&counters, sizeof(unsigned) * 16, stream);
         AMFLS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned) * 16, stream));
         AMFLS_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventBlockingSync));

@@ -7,7 +7,6 @@
 namespace amfls_gpu {
 namespace {
 
-constexpr int kGrid = 1216;
 constexpr int kThreads = 256;
 
 __global__ void max_pass_kernel(VectorSet set, NormResult* out, double* partials,
@@ -85,7 +84,7 @@ void norm_passes(const VectorSet& set, NormResult* out, double* partials, unsign
                  cudaStream_t stream) {
     long long longest = 1;
     for (int i = 0; i < set.count; ++i) longest = std::max(longest, set.n[i]);
-    const int grid = (int)std::max<long long>(1, std::min<long long>(kGrid, (longest + 1023) / 1024));
+    const int grid = (int)std::max<long long>(1, std::min<long long>(grid_cap(), (longest + 1023) / 1024));
     max_pass_kernel<<<grid, kThreads, 0, stream>>>(set, out, partials, counter);
     AMFLS_LAUNCHED();
     sum_pass_kernel<<<grid, kThreads, 0, stream>>>(set, out, partials, counter);

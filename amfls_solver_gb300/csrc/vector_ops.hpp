@@ -29,7 +29,7 @@ struct VectorSet {
 };
 
 // Both passes; results land in device `out`.  `partials` must hold
-// 2 * kMaxVectors * 1216 doubles and `counter` one zeroed unsigned.
+// 2 * kMaxVectors * kMaxGridCap doubles and `counter` one zeroed unsigned.
 void norm_passes(const VectorSet& set, NormResult* out, double* partials, unsigned* counter,
                  cudaStream_t stream);
 

@@ -4,8 +4,10 @@
 //   begin        decide on the device whether the level runs (can_advance,
 //                depth target); reset the step audit
 //   A^T u        fused SpMV^T: r = A^T u - beta v_prev, ||A^T u||, ||r||
-//   V^T r        c1, per-panel partials reduced by the last block per panel
-//   r -= V c1    with ||r||; its last block takes the DGKS decision
+//   V^T r        c1: warp tasks (panel, row chunk), chunks added in order by
+//                the warp that finishes a panel last
+//   r -= V c1    warp tasks (row tile, panel group), with ||r||; the warp
+//                that finishes the last tile takes the DGKS decision
 //                (second pass only if ||r_after|| < sqrt(1/2) ||r_before||,
 //                krylov_workspace.cpp:152-165) and, when no second pass is
 //                needed, the rank decision against the cutoff
@@ -72,7 +74,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr double kEps = 2.220446049250313e-16;
-constexpr int kGemvTargetBlocks = 152 * 16;
+// per-block partials of the reductions sized for up to 16 blocks per SM
+constexpr int kMaxGemvTargetBlocks = 16 * 256;
 
 enum Hook { kHookNone = 0, kHookRightPass1 = 1, kHookRightPass2 = 2 };
 
@@ -248,81 +251,6 @@ __global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, i
     }
 }
 
-// c = V^T r, masked to k columns.  grid (panels, chunks); partials [P][C][32].
-__global__ void __launch_bounds__(kThreads)
-vt_r_kernel(double* const* __restrict__ panels, int n, int chunk_rows,
-            const double* __restrict__ r, double* __restrict__ c, double* partials,
-            unsigned* panel_tickets, DevState* st, int pass) {
-    if (!st->go || (pass == 2 && !st->second_pass)) return;
-    const int k = st->k;  // k == 0: no projection (decided in right_scales_kernel)
-    const int p = blockIdx.x, chunk = blockIdx.y, nchunks = gridDim.y;
-    if (p * 32 >= k) return;  // panel beyond the current basis
-    const double* __restrict__ vp = panels[p];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int q = lane & 3, rsub = lane >> 2;
-    const long long row0 = (long long)chunk * chunk_rows;
-    const long long row1 = min((long long)n, row0 + chunk_rows);
-    double acc[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
-    for (long long base = row0 + warp * 8; base < row1; base += 64) {
-        const long long row = base + rsub;
-        if (row < row1) {
-            const double2* src = reinterpret_cast<const double2*>(vp + row * 32 + q * 8);
-            const double2 a0 = __ldg(src), a1 = __ldg(src + 1), a2 = __ldg(src + 2),
-                          a3 = __ldg(src + 3);
-            const double rv = __ldg(r + row);
-            acc[0] = fma(a0.x, rv, acc[0]);
-            acc[1] = fma(a0.y, rv, acc[1]);
-            acc[2] = fma(a1.x, rv, acc[2]);
-            acc[3] = fma(a1.y, rv, acc[3]);
-            acc[4] = fma(a2.x, rv, acc[4]);
-            acc[5] = fma(a2.y, rv, acc[5]);
-            acc[6] = fma(a3.x, rv, acc[6]);
-            acc[7] = fma(a3.y, rv, acc[7]);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 4);
-        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 8);
-        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 16);
-    }
-    __shared__ double sm[8][32];
-    __shared__ bool last;
-    if (lane < 4) {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) sm[warp][lane * 8 + i] = acc[i];
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double s = 0.0;
-#pragma unroll
-        for (int w = 0; w < 8; ++w) s += sm[w][threadIdx.x];
-        partials[((long long)p * nchunks + chunk) * 32 + threadIdx.x] = s;
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned t = atomicAdd(&panel_tickets[p], 1u);
-        last = (t == (unsigned)nchunks - 1);
-        if (last) panel_tickets[p] = 0u;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (threadIdx.x < 32) {
-        double s = 0.0;
-        for (int ch = 0; ch < nchunks; ++ch)
-            s += partials[((long long)p * nchunks + ch) * 32 + threadIdx.x];
-        const int col = p * 32 + threadIdx.x;
-        if (col < k) {
-            c[col] = s;
-            if (!isfinite(s)) st->coeff_nonfinite = 1;
-        }
-    }
-}
-
 // out = r - V c (subtract) or out = V c; 32 rows per block, warps split the
 // panels.  Sum of squares of out reduced by the last block, then `hook`.
 __global__ void __launch_bounds__(kThreads)
@@ -408,6 +336,232 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
             }
         }
     }
+}
+
+// ----------------------------------------------------------------------------
+// Basis sweeps of the width-one levels as warp tasks.  Every V element costs
+// one FP64 FMA and this GPU retires two lanes' FP64 FMAs per SM clock, so a
+// sweep is bound by the FP64 pipe (about 5 TB/s of V), not by HBM; the layout
+// keeps FP64 instructions to the FMAs themselves:
+//   * V^T r: a warp task is (panel p, chunk of rows); lane l owns column
+//     p*32 + l and sums V[row][l] r[row] down the chunk as one FMA chain (a
+//     warp load reads one whole 256-byte panel row); the chunks of a panel
+//     are added in chunk order by the warp that finishes the panel last
+//     (atomic ticket per panel);
+//   * r - V c: a warp task is (tile of 32 rows, group of panels); lane l owns
+//     row t*32 + l and sums V[row][col] c[col] along the row as one FMA
+//     chain; a tile's groups are added in group order by the warp that
+//     finishes the tile last, which also writes the tile's sum of squares;
+//     the warp that finishes the last tile adds those in tile order and
+//     takes the DGKS decision.
+// Tasks are dealt to warps in contiguous balanced ranges, and every sum runs
+// in an order fixed by (n, k, grid), so results are deterministic.
+constexpr int kSweepTargetTasksPerWarp = 8;
+
+struct SweepShape {
+    int P;       // panels in use
+    int chunks;  // V^T r: row chunks per panel
+    int chunk_rows;
+    int T;       // r - V c: row tiles
+    int G;       // r - V c: panel groups per tile
+    int Pg;      // panels per group
+};
+
+__device__ inline SweepShape sweep_shape(int n, int k, int warps) {
+    SweepShape sh;
+    sh.P = (k + 31) / 32;
+    const long long target = (long long)kSweepTargetTasksPerWarp * warps;
+    int chunks = sh.P > 0 ? (int)min((target + sh.P - 1) / sh.P, ((long long)n + 255) / 256) : 1;
+    chunks = max(1, chunks);
+    int rows = (int)(((long long)n + chunks - 1) / chunks);
+    rows = (rows + 31) / 32 * 32;
+    sh.chunk_rows = rows;
+    sh.chunks = (n + rows - 1) / rows;
+    sh.T = (n + 31) / 32;
+    const int gmax = max(1, sh.P / 4);  // at least four panels per task
+    int G = (int)min(max(1LL, (target + sh.T - 1) / sh.T), (long long)gmax);
+    sh.Pg = sh.P > 0 ? (sh.P + G - 1) / G : 1;
+    sh.G = sh.P > 0 ? (sh.P + sh.Pg - 1) / sh.Pg : 1;
+    return sh;
+}
+
+// the contiguous range of tasks of warp w among W warps
+__device__ inline void warp_range(long long tasks, int w, int W, long long& t0, long long& t1) {
+    t0 = tasks * w / W;
+    t1 = tasks * (w + 1) / W;
+}
+
+__global__ void __launch_bounds__(kThreads)
+sweep_vt_kernel(double* const* __restrict__ panels, int n, const double* __restrict__ r,
+                double* __restrict__ c, double* __restrict__ part, unsigned* panel_tickets,
+                DevState* st, int pass) {
+    if (!st->go || (pass == 2 && !st->second_pass)) return;
+    const int k = st->k;
+    const int lane = threadIdx.x & 31;
+    const int W = gridDim.x * (blockDim.x >> 5);
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const SweepShape sh = sweep_shape(n, k, W);
+    long long t0, t1;
+    warp_range((long long)sh.P * sh.chunks, w, W, t0, t1);
+    for (long long t = t0; t < t1; ++t) {
+        const int p = (int)(t / sh.chunks), ch = (int)(t - (long long)p * sh.chunks);
+        const double* __restrict__ vp = panels[p] + lane;
+        const int row0 = ch * sh.chunk_rows, row1 = min(n, row0 + sh.chunk_rows);
+        double acc = 0.0;
+        for (int base = row0; base < row1; base += 32) {
+            const int cnt = min(32, row1 - base);
+            const double rv = lane < cnt ? __ldg(r + base + lane) : 0.0;
+            if (cnt == 32) {
+#pragma unroll
+                for (int j0 = 0; j0 < 32; j0 += 8) {
+                    double v[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) v[j] = __ldg(vp + (long long)(base + j0 + j) * 32);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        acc = fma(v[j], __shfl_sync(0xffffffffu, rv, j0 + j), acc);
+                }
+            } else {
+                for (int j = 0; j < cnt; ++j)
+                    acc = fma(__ldg(vp + (long long)(base + j) * 32),
+                              __shfl_sync(0xffffffffu, rv, j), acc);
+            }
+        }
+        part[((long long)p * sh.chunks + ch) * 32 + lane] = acc;
+        __threadfence();
+        __syncwarp();
+        unsigned ticket = 0;
+        if (lane == 0) ticket = atomicAdd(&panel_tickets[p], 1u);
+        ticket = __shfl_sync(0xffffffffu, ticket, 0);
+        if (ticket != (unsigned)sh.chunks - 1) continue;
+        __threadfence();
+        double s = 0.0;
+        for (int j = 0; j < sh.chunks; ++j) s += __ldcg(part + ((long long)p * sh.chunks + j) * 32 + lane);
+        const int col = p * 32 + lane;
+        if (col < k) {
+            c[col] = s;
+            if (!isfinite(s)) st->coeff_nonfinite = 1;
+        }
+        if (lane == 0) panel_tickets[p] = 0u;
+    }
+}
+
+// The DGKS test and rank decision after the right residual's norm is known
+// (the hooks of v_c_kernel).
+__device__ inline void finish_right_norm(DevState* st, int hook, double sumsq, int m, int n) {
+    st->norm_after = sqrt(sumsq);
+    if (hook == kHookRightPass1) {
+        const double before = st->norm_before, after = st->norm_after;
+        const bool again = isfinite(before) && isfinite(after) && after < 0.70710678118654757 * before;
+        st->second_pass = again ? 1 : 0;
+        if (!again) decide_right(st, m, n);
+    } else if (hook == kHookRightPass2) {
+        decide_right(st, m, n);
+    }
+}
+
+// out = r_in - V c (subtract) or V c over the current basis, its sum of
+// squares, then `hook`.
+__global__ void __launch_bounds__(kThreads)
+sweep_vc_kernel(double* const* __restrict__ panels, int n, const double* __restrict__ c,
+                const double* r_in, double* out, int subtract, double* __restrict__ part,
+                double* __restrict__ tile_sq, unsigned* tile_tickets, unsigned* done, DevState* st,
+                int hook, int m_rows, int pass) {
+    if (!st->go || (pass == 2 && !st->second_pass) || st->k == 0) return;
+    const int k = st->k;
+    const int lane = threadIdx.x & 31;
+    const int W = gridDim.x * (blockDim.x >> 5);
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const SweepShape sh = sweep_shape(n, k, W);
+    long long t0, t1;
+    warp_range((long long)sh.T * sh.G, w, W, t0, t1);
+    for (long long t = t0; t < t1; ++t) {
+        const int tile = (int)(t / sh.G), g = (int)(t - (long long)tile * sh.G);
+        const int row = tile * 32 + lane;
+        const int p0 = g * sh.Pg, p1 = min(sh.P, p0 + sh.Pg);
+        double acc = 0.0;
+        if (row < n) {
+            for (int p = p0; p < p1; ++p) {
+                const double2* __restrict__ src =
+                    reinterpret_cast<const double2*>(panels[p] + (long long)row * 32);
+                const double* cp = c + p * 32;
+                const int valid = min(32, k - p * 32);
+                double2 v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = __ldg(src + j);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const double c0 = 2 * j < valid ? cp[2 * j] : 0.0;
+                    const double c1 = 2 * j + 1 < valid ? cp[2 * j + 1] : 0.0;
+                    acc = fma(v[j].x, c0, acc);
+                    acc = fma(v[j].y, c1, acc);
+                }
+            }
+        }
+        double y = acc;
+        if (sh.G > 1) {
+            part[((long long)tile * sh.G + g) * 32 + lane] = acc;
+            __threadfence();
+            __syncwarp();
+            unsigned ticket = 0;
+            if (lane == 0) ticket = atomicAdd(&tile_tickets[tile], 1u);
+            ticket = __shfl_sync(0xffffffffu, ticket, 0);
+            if (ticket != (unsigned)sh.G - 1) continue;
+            __threadfence();
+            y = 0.0;
+            for (int j = 0; j < sh.G; ++j) y += __ldcg(part + ((long long)tile * sh.G + j) * 32 + lane);
+            if (lane == 0) tile_tickets[tile] = 0u;
+        }
+        double sq = 0.0;
+        if (row < n) {
+            const double o = subtract ? r_in[row] - y : y;
+            out[row] = o;
+            sq = o * o;
+        }
+        if (hook == kHookNone) continue;
+        sq = warp_sum(sq);
+        if (lane == 0) tile_sq[tile] = sq;
+        __threadfence();
+        __syncwarp();
+        unsigned fin = 0;
+        if (lane == 0) fin = atomicAdd(done, 1u);
+        fin = __shfl_sync(0xffffffffu, fin, 0);
+        if (fin != (unsigned)sh.T - 1) continue;
+        __threadfence();
+        double a = 0.0;
+        for (int j = lane; j < sh.T; j += 32) a += __ldcg(tile_sq + j);
+        a = warp_sum(a);
+        if (lane == 0) {
+            *done = 0u;
+            finish_right_norm(st, hook, a, m_rows, n);
+        }
+    }
+}
+
+// Grid of the sweep kernels: every block resident at once (so the balanced
+// task ranges are balanced per SM), set up once per device.
+int sweep_grid() {
+    static int cached[64] = {};
+    int dev = 0;
+    AMFLS_CUDA(cudaGetDevice(&dev));
+    const int slot = dev >= 0 && dev < 64 ? dev : 0;
+    int g = __atomic_load_n(&cached[slot], __ATOMIC_RELAXED);
+    if (g == 0) {
+        int a = 0, b = 0;
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, sweep_vt_kernel, kThreads, 0));
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_vc_kernel, kThreads, 0));
+        g = std::max(1, std::min(a, b)) * sm_count();
+        __atomic_store_n(&cached[slot], g, __ATOMIC_RELAXED);
+    }
+    return g;
+}
+
+// Partial-sum doubles the sweeps need for n rows and up to `panels` panels
+// on a grid of `grid` blocks (the task bounds of sweep_shape).
+long long sweep_part_doubles(int n, long long panels, int grid) {
+    const long long W = (long long)grid * (kThreads / 32);
+    const long long tiles = (n + 31) / 32;
+    return (kSweepTargetTasksPerWarp * W + std::max(panels, tiles) + 1) * 32;
 }
 
 __global__ void normalize_right_kernel(const double* r, int n, double* const* panels,
@@ -642,9 +796,18 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     // scratch: V^T r partials ((target blocks + panels) x 32), then the
     // per-block norm partials of the V c sweep (n/32 + slack)
     const long long max_panels = basis_limit_ / 32 + 2;
-    vc_partials_offset_ = (kGemvTargetBlocks + max_panels) * 32 + 6 * 1216;
+    vc_partials_offset_ = (kMaxGemvTargetBlocks + max_panels) * 32 + 6 * kMaxGridCap;
     const long long pcount = vc_partials_offset_ + (n_ + 31) / 32 + 1024;
     stream_alloc(&partials_, sizeof(double) * pcount, stream_);
+    sweep_grid_ = sweep_grid();
+    sweep_panels_ = max_panels;
+    const long long tiles = (n_ + 31) / 32;
+    stream_alloc(&sweep_part_, sizeof(double) * sweep_part_doubles(n_, max_panels, sweep_grid_),
+                 stream_);
+    stream_alloc(&sweep_sq_, sizeof(double) * tiles, stream_);
+    stream_alloc(&sweep_tickets_, sizeof(unsigned) * (max_panels + tiles + 1), stream_);
+    AMFLS_CUDA(cudaMemsetAsync(sweep_tickets_, 0, sizeof(unsigned) * (max_panels + tiles + 1),
+                               stream_));
     const long long ncounters = 64 + max_panels + 64;
     stream_alloc(&counter_, sizeof(unsigned) * ncounters, stream_);
     AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * ncounters, stream_));
@@ -671,6 +834,9 @@ Workspace::~Workspace() {
     stream_free(dstate_, stream_);
     stream_free(red_, stream_);
     stream_free(partials_, stream_);
+    stream_free(sweep_part_, stream_);
+    stream_free(sweep_sq_, stream_);
+    stream_free(sweep_tickets_, stream_);
     stream_free(counter_, stream_);
     stream_free(R_, stream_);
     stream_free(vnew_, stream_);
@@ -772,7 +938,7 @@ void Workspace::initialize(const double* d_aux, int aux_cols) {
     ensure_t_capacity(64);
     if (std::isfinite(b_norm_) && b_norm_ > 0.0 && basis_limit_ > 0) {
         const double inv = 1.0 / b_norm_;
-        scale_copy_kernel<<<std::max<long long>(1, std::min<long long>(1216, (m_ + 255) / 256)), 256, 0,
+        scale_copy_kernel<<<std::max<long long>(1, std::min<long long>(grid_cap(), (m_ + 255) / 256)), 256, 0,
                             stream_>>>(b_, U_, m_, inv);
         AMFLS_LAUNCHED();
         AMFLS_CUDA(cudaMemcpyAsync(g_, &b_norm_, sizeof(double), cudaMemcpyHostToDevice, stream_));
@@ -805,22 +971,22 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     if (!op_.product1(true, U_, ep, s)) throw std::runtime_error("operator has no fused device product");
     right_scales_kernel<<<1, 32, 0, s>>>(dstate_, &red_[0], m_, n_);
     AMFLS_LAUNCHED();
-    const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
-    const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + pcap - 1) / pcap));
-    const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
-    const dim3 tgrid(pcap, chunks);
-    const int ngrid = (int)((n_ + 31) / 32);
+    (void)pcap;  // the sweeps take their task shapes from k on the device
+    const long long tiles = (n_ + 31) / 32;
+    unsigned* panel_tickets = sweep_tickets_;
+    unsigned* tile_tickets = sweep_tickets_ + sweep_panels_;
+    unsigned* done = tile_tickets + tiles;
     for (int pass = 1; pass <= 2; ++pass) {
         double* c = pass == 1 ? c1_ : c2_;
-        vt_r_kernel<<<tgrid, kThreads, 0, s>>>(V_->device_table(), n_, chunk_rows, R_, c, partials_,
-                                               counter_ + 64, dstate_, pass);
+        sweep_vt_kernel<<<sweep_grid_, kThreads, 0, s>>>(V_->device_table(), n_, R_, c,
+                                                         sweep_part_, panel_tickets, dstate_, pass);
         AMFLS_LAUNCHED();
-        v_c_kernel<<<ngrid, kThreads, 0, s>>>(
-            V_->device_table(), n_, -1, c, R_, R_, 1, partials_ + vc_partials_offset_, counter_ + 3,
-            dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, 1, pass);
+        sweep_vc_kernel<<<sweep_grid_, kThreads, 0, s>>>(
+            V_->device_table(), n_, c, R_, R_, 1, sweep_part_, sweep_sq_, tile_tickets, done,
+            dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, pass);
         AMFLS_LAUNCHED();
     }
-    normalize_right_kernel<<<(int)std::min<long long>(1216, (n_ + 255) / 256), 256, 0, s>>>(
+    normalize_right_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0, s>>>(
         R_, n_, V_->device_table(), vnew_, dstate_);
     AMFLS_LAUNCHED();
     // y = A v - ||r|| u, with ||A v||, ||y||, u.y
@@ -835,14 +1001,14 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     el.partials = partials_;
     el.counter = counter_ + 2;
     op_.product1(false, vnew_, el, s);
-    const int lgrid = (int)std::max<long long>(1, std::min<long long>(1216, (m_ + 1023) / 1024));
+    const int lgrid = (int)std::max<long long>(1, std::min<long long>(grid_cap(), (m_ + 1023) / 1024));
     for (int pass = 1; pass <= 2; ++pass) {
         left_pass_kernel<<<lgrid, kThreads, 0, s>>>(Y_, U_, b_, m_, &red_[1], partials_,
                                                     counter_ + 4, dstate_, pass, n_, alpha_, beta_,
                                                     g_);
         AMFLS_LAUNCHED();
     }
-    normalize_left_kernel<<<(int)std::min<long long>(1216, (m_ + 255) / 256), 256, 0, s>>>(
+    normalize_left_kernel<<<(int)std::min<long long>(grid_cap(), (m_ + 255) / 256), 256, 0, s>>>(
         Y_, U_, m_, dstate_);
     AMFLS_LAUNCHED();
 }
@@ -990,21 +1156,21 @@ __global__ void probe_fill_kernel(double* const* panels, int n, int k, double* r
 void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double seconds[2]) {
     if (n <= 0 || k <= 0 || reps <= 0) throw std::invalid_argument("probe sizes must be positive");
     const int P = (k + 31) / 32;
-    int pcap = 4;
-    while (pcap < P) pcap *= 2;
-    PanelStore V(n, pcap, s);
+    PanelStore V(n, P, s);
     V.ensure_columns(k);
-    double *r = nullptr, *w = nullptr, *c = nullptr, *partials = nullptr;
-    unsigned* counters = nullptr;
+    const int grid = sweep_grid();
+    const long long tiles = (n + 31) / 32;
+    double *r = nullptr, *w = nullptr, *c = nullptr, *part = nullptr, *sq = nullptr;
+    unsigned* tickets = nullptr;
     DevState* st = nullptr;
-    const long long vc_off = (long long)(kGemvTargetBlocks + pcap) * 32 + 6 * 1216;
     stream_alloc(&r, sizeof(double) * n, s);
     stream_alloc(&w, sizeof(double) * n, s);
-    stream_alloc(&c, sizeof(double) * 32 * pcap, s);
-    stream_alloc(&partials, sizeof(double) * (vc_off + (n + 31) / 32 + 1024), s);
-    stream_alloc(&counters, sizeof(unsigned) * (64 + pcap + 64), s);
+    stream_alloc(&c, sizeof(double) * 32 * P, s);
+    stream_alloc(&part, sizeof(double) * sweep_part_doubles(n, P, grid), s);
+    stream_alloc(&sq, sizeof(double) * tiles, s);
+    stream_alloc(&tickets, sizeof(unsigned) * (P + tiles + 1), s);
     stream_alloc(&st, sizeof(DevState), s);
-    AMFLS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned) * (64 + pcap + 64), s));
+    AMFLS_CUDA(cudaMemsetAsync(tickets, 0, sizeof(unsigned) * (P + tiles + 1), s));
     DevState h;
     std::memset(&h, 0, sizeof(h));
     h.k = k;
@@ -1014,22 +1180,16 @@ void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double se
     h.right_scale = 1.0;
     h.norm_before = 1e300;  // the pass never decides the level: state stays as set
     AMFLS_CUDA(cudaMemcpyAsync(st, &h, sizeof(DevState), cudaMemcpyHostToDevice, s));
-    probe_fill_kernel<<<1216, 256, 0, s>>>(V.device_table(), n, k, r);
+    probe_fill_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), n, k, r);
     AMFLS_LAUNCHED();
-    const int max_chunks = (int)std::max<long long>(1, (n + 255) / 256);
-    const int chunks = std::max(1, std::min(max_chunks, (kGemvTargetBlocks + pcap - 1) / pcap));
-    const int chunk_rows = (int)(((long long)n + chunks - 1) / chunks);
-    const dim3 tgrid(pcap, chunks);
-    const int ngrid = (int)((n + 31) / 32);
     auto vt = [&] {
-        vt_r_kernel<<<tgrid, kThreads, 0, s>>>(V.device_table(), n, chunk_rows, r, c, partials,
-                                               counters + 64, st, 1);
+        sweep_vt_kernel<<<grid, kThreads, 0, s>>>(V.device_table(), n, r, c, part, tickets, st, 1);
         AMFLS_LAUNCHED();
     };
     auto vc = [&] {
-        v_c_kernel<<<ngrid, kThreads, 0, s>>>(V.device_table(), n, -1, c, r, w, 0,
-                                              partials + vc_off, counters + 3, st,
-                                              kHookRightPass1, n, 1, 1);
+        sweep_vc_kernel<<<grid, kThreads, 0, s>>>(V.device_table(), n, c, r, w, 0, part, sq,
+                                                  tickets + P, tickets + P + tiles, st,
+                                                  kHookRightPass1, n, 1);
         AMFLS_LAUNCHED();
     };
     cudaEvent_t e[3];
@@ -1053,8 +1213,9 @@ void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double se
     stream_free(r, s);
     stream_free(w, s);
     stream_free(c, s);
-    stream_free(partials, s);
-    stream_free(counters, s);
+    stream_free(part, s);
+    stream_free(sq, s);
+    stream_free(tickets, s);
     stream_free(st, s);
     stream_wait(s);
 }

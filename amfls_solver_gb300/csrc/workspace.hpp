@@ -153,6 +153,13 @@ private:
     RedResult* red_ = nullptr;  // [4] reduction slots
     double* partials_ = nullptr;
     long long vc_partials_offset_ = 0;
+    // basis sweeps (sweep_vt_kernel / sweep_vc_kernel): their grid, partial
+    // sums, per-tile sums of squares and tickets (panels | tiles | done)
+    int sweep_grid_ = 0;
+    double* sweep_part_ = nullptr;
+    double* sweep_sq_ = nullptr;
+    unsigned* sweep_tickets_ = nullptr;
+    long long sweep_panels_ = 0;
     unsigned* counter_ = nullptr;   // self-resetting tickets: misc + one per V panel
 
     std::unique_ptr<PanelStore> V_;
