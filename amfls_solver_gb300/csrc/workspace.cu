@@ -74,8 +74,15 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr double kEps = 2.220446049250313e-16;
-// per-block partials of the reductions sized for up to 16 blocks per SM
+// V^T r by blocks (vt_r_kernel) launches about 16 blocks per SM (panels x
+// row chunks); kMaxGemvTargetBlocks bounds it for sizing the partials
+inline int gemv_target_blocks() { return 16 * sm_count(); }
 constexpr int kMaxGemvTargetBlocks = 16 * 256;
+
+// Tall bases (n rows at least this) keep the block sweeps vt_r_kernel /
+// v_c_kernel, which run closest to the FP64 roof there; shorter ones use the
+// warp-task sweeps, whose grid does not shrink with n.
+constexpr int kWarpSweepMaxRows = 1 << 17;
 
 enum Hook { kHookNone = 0, kHookRightPass1 = 1, kHookRightPass2 = 2 };
 
@@ -251,6 +258,81 @@ __global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, i
     }
 }
 
+// c = V^T r, masked to k columns.  grid (panels, chunks); partials [P][C][32].
+__global__ void __launch_bounds__(kThreads)
+vt_r_kernel(double* const* __restrict__ panels, int n, int chunk_rows,
+            const double* __restrict__ r, double* __restrict__ c, double* partials,
+            unsigned* panel_tickets, DevState* st, int pass) {
+    if (!st->go || (pass == 2 && !st->second_pass)) return;
+    const int k = st->k;  // k == 0: no projection (decided in right_scales_kernel)
+    const int p = blockIdx.x, chunk = blockIdx.y, nchunks = gridDim.y;
+    if (p * 32 >= k) return;  // panel beyond the current basis
+    const double* __restrict__ vp = panels[p];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int q = lane & 3, rsub = lane >> 2;
+    const long long row0 = (long long)chunk * chunk_rows;
+    const long long row1 = min((long long)n, row0 + chunk_rows);
+    double acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    for (long long base = row0 + warp * 8; base < row1; base += 64) {
+        const long long row = base + rsub;
+        if (row < row1) {
+            const double2* src = reinterpret_cast<const double2*>(vp + row * 32 + q * 8);
+            const double2 a0 = __ldg(src), a1 = __ldg(src + 1), a2 = __ldg(src + 2),
+                          a3 = __ldg(src + 3);
+            const double rv = __ldg(r + row);
+            acc[0] = fma(a0.x, rv, acc[0]);
+            acc[1] = fma(a0.y, rv, acc[1]);
+            acc[2] = fma(a1.x, rv, acc[2]);
+            acc[3] = fma(a1.y, rv, acc[3]);
+            acc[4] = fma(a2.x, rv, acc[4]);
+            acc[5] = fma(a2.y, rv, acc[5]);
+            acc[6] = fma(a3.x, rv, acc[6]);
+            acc[7] = fma(a3.y, rv, acc[7]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 4);
+        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 8);
+        acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 16);
+    }
+    __shared__ double sm[8][32];
+    __shared__ bool last;
+    if (lane < 4) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) sm[warp][lane * 8 + i] = acc[i];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += sm[w][threadIdx.x];
+        partials[((long long)p * nchunks + chunk) * 32 + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned t = atomicAdd(&panel_tickets[p], 1u);
+        last = (t == (unsigned)nchunks - 1);
+        if (last) panel_tickets[p] = 0u;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (int ch = 0; ch < nchunks; ++ch)
+            s += partials[((long long)p * nchunks + ch) * 32 + threadIdx.x];
+        const int col = p * 32 + threadIdx.x;
+        if (col < k) {
+            c[col] = s;
+            if (!isfinite(s)) st->coeff_nonfinite = 1;
+        }
+    }
+}
+
 // out = r - V c (subtract) or out = V c; 32 rows per block, warps split the
 // panels.  Sum of squares of out reduced by the last block, then `hook`.
 __global__ void __launch_bounds__(kThreads)
@@ -371,7 +453,7 @@ __device__ inline SweepShape sweep_shape(int n, int k, int warps) {
     SweepShape sh;
     sh.P = (k + 31) / 32;
     const long long target = (long long)kSweepTargetTasksPerWarp * warps;
-    int chunks = sh.P > 0 ? (int)min((target + sh.P - 1) / sh.P, ((long long)n + 255) / 256) : 1;
+    int chunks = sh.P > 0 ? (int)min((target + sh.P - 1) / sh.P, ((long long)n + 127) / 128) : 1;
     chunks = max(1, chunks);
     int rows = (int)(((long long)n + chunks - 1) / chunks);
     rows = (rows + 31) / 32 * 32;
@@ -389,6 +471,23 @@ __device__ inline SweepShape sweep_shape(int n, int k, int warps) {
 __device__ inline void warp_range(long long tasks, int w, int W, long long& t0, long long& t1) {
     t0 = tasks * w / W;
     t1 = tasks * (w + 1) / W;
+}
+
+// the warp that takes the last ticket: sum `count` partials spaced `stride`
+// apart, in index order, with eight loads in flight (L2 reads; the writers
+// were other SMs)
+__device__ inline double ordered_sum(const double* p, int count, long long stride) {
+    double s = 0.0;
+    int j = 0;
+    for (; j + 8 <= count; j += 8) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(p + (long long)(j + u) * stride);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (; j < count; ++j) s += __ldcg(p + (long long)j * stride);
+    return s;
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -413,12 +512,12 @@ sweep_vt_kernel(double* const* __restrict__ panels, int n, const double* __restr
             const double rv = lane < cnt ? __ldg(r + base + lane) : 0.0;
             if (cnt == 32) {
 #pragma unroll
-                for (int j0 = 0; j0 < 32; j0 += 8) {
-                    double v[8];
+                for (int j0 = 0; j0 < 32; j0 += 16) {
+                    double v[16];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) v[j] = __ldg(vp + (long long)(base + j0 + j) * 32);
+                    for (int j = 0; j < 16; ++j) v[j] = __ldg(vp + (long long)(base + j0 + j) * 32);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
+                    for (int j = 0; j < 16; ++j)
                         acc = fma(v[j], __shfl_sync(0xffffffffu, rv, j0 + j), acc);
                 }
             } else {
@@ -435,8 +534,7 @@ sweep_vt_kernel(double* const* __restrict__ panels, int n, const double* __restr
         ticket = __shfl_sync(0xffffffffu, ticket, 0);
         if (ticket != (unsigned)sh.chunks - 1) continue;
         __threadfence();
-        double s = 0.0;
-        for (int j = 0; j < sh.chunks; ++j) s += __ldcg(part + ((long long)p * sh.chunks + j) * 32 + lane);
+        const double s = ordered_sum(part + (long long)p * sh.chunks * 32 + lane, sh.chunks, 32);
         const int col = p * 32 + lane;
         if (col < k) {
             c[col] = s;
@@ -508,8 +606,7 @@ sweep_vc_kernel(double* const* __restrict__ panels, int n, const double* __restr
             ticket = __shfl_sync(0xffffffffu, ticket, 0);
             if (ticket != (unsigned)sh.G - 1) continue;
             __threadfence();
-            y = 0.0;
-            for (int j = 0; j < sh.G; ++j) y += __ldcg(part + ((long long)tile * sh.G + j) * 32 + lane);
+            y = ordered_sum(part + (long long)tile * sh.G * 32 + lane, sh.G, 32);
             if (lane == 0) tile_tickets[tile] = 0u;
         }
         double sq = 0.0;
@@ -971,20 +1068,35 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     if (!op_.product1(true, U_, ep, s)) throw std::runtime_error("operator has no fused device product");
     right_scales_kernel<<<1, 32, 0, s>>>(dstate_, &red_[0], m_, n_);
     AMFLS_LAUNCHED();
-    (void)pcap;  // the sweeps take their task shapes from k on the device
     const long long tiles = (n_ + 31) / 32;
     unsigned* panel_tickets = sweep_tickets_;
     unsigned* tile_tickets = sweep_tickets_ + sweep_panels_;
     unsigned* done = tile_tickets + tiles;
+    const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
+    const int chunks = std::max(1, std::min(max_chunks, (gemv_target_blocks() + pcap - 1) / pcap));
+    const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
     for (int pass = 1; pass <= 2; ++pass) {
         double* c = pass == 1 ? c1_ : c2_;
-        sweep_vt_kernel<<<sweep_grid_, kThreads, 0, s>>>(V_->device_table(), n_, R_, c,
-                                                         sweep_part_, panel_tickets, dstate_, pass);
-        AMFLS_LAUNCHED();
-        sweep_vc_kernel<<<sweep_grid_, kThreads, 0, s>>>(
-            V_->device_table(), n_, c, R_, R_, 1, sweep_part_, sweep_sq_, tile_tickets, done,
-            dstate_, pass == 1 ? kHookRightPass1 : kHookRightPass2, m_, pass);
-        AMFLS_LAUNCHED();
+        const int hook = pass == 1 ? kHookRightPass1 : kHookRightPass2;
+        if (n_ < kWarpSweepMaxRows) {
+            sweep_vt_kernel<<<sweep_grid_, kThreads, 0, s>>>(V_->device_table(), n_, R_, c,
+                                                             sweep_part_, panel_tickets, dstate_,
+                                                             pass);
+            AMFLS_LAUNCHED();
+            sweep_vc_kernel<<<sweep_grid_, kThreads, 0, s>>>(
+                V_->device_table(), n_, c, R_, R_, 1, sweep_part_, sweep_sq_, tile_tickets, done,
+                dstate_, hook, m_, pass);
+            AMFLS_LAUNCHED();
+        } else {
+            vt_r_kernel<<<dim3(pcap, chunks), kThreads, 0, s>>>(V_->device_table(), n_, chunk_rows,
+                                                                R_, c, partials_, counter_ + 64,
+                                                                dstate_, pass);
+            AMFLS_LAUNCHED();
+            v_c_kernel<<<(int)tiles, kThreads, 0, s>>>(
+                V_->device_table(), n_, -1, c, R_, R_, 1, partials_ + vc_partials_offset_,
+                counter_ + 3, dstate_, hook, m_, 1, pass);
+            AMFLS_LAUNCHED();
+        }
     }
     normalize_right_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0, s>>>(
         R_, n_, V_->device_table(), vnew_, dstate_);
@@ -1182,14 +1294,29 @@ void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double se
     AMFLS_CUDA(cudaMemcpyAsync(st, &h, sizeof(DevState), cudaMemcpyHostToDevice, s));
     probe_fill_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), n, k, r);
     AMFLS_LAUNCHED();
+    const bool warp_sweeps = n < kWarpSweepMaxRows;  // as enqueue_level_kernels chooses
+    int pcap = 4;
+    while (pcap < P) pcap *= 2;
+    const int max_chunks = (int)std::max<long long>(1, (n + 255) / 256);
+    const int chunks = std::max(1, std::min(max_chunks, (gemv_target_blocks() + pcap - 1) / pcap));
+    const int chunk_rows = (int)(((long long)n + chunks - 1) / chunks);
     auto vt = [&] {
-        sweep_vt_kernel<<<grid, kThreads, 0, s>>>(V.device_table(), n, r, c, part, tickets, st, 1);
+        if (warp_sweeps)
+            sweep_vt_kernel<<<grid, kThreads, 0, s>>>(V.device_table(), n, r, c, part, tickets, st,
+                                                      1);
+        else
+            vt_r_kernel<<<dim3(P, chunks), kThreads, 0, s>>>(V.device_table(), n, chunk_rows, r, c,
+                                                             part, tickets, st, 1);
         AMFLS_LAUNCHED();
     };
     auto vc = [&] {
-        sweep_vc_kernel<<<grid, kThreads, 0, s>>>(V.device_table(), n, c, r, w, 0, part, sq,
-                                                  tickets + P, tickets + P + tiles, st,
-                                                  kHookRightPass1, n, 1);
+        if (warp_sweeps)
+            sweep_vc_kernel<<<grid, kThreads, 0, s>>>(V.device_table(), n, c, r, w, 0, part, sq,
+                                                      tickets + P, tickets + P + tiles, st,
+                                                      kHookRightPass1, n, 1);
+        else
+            v_c_kernel<<<(int)tiles, kThreads, 0, s>>>(V.device_table(), n, -1, c, r, w, 0, part,
+                                                       tickets + P, st, kHookRightPass1, n, 1, 1);
         AMFLS_LAUNCHED();
     };
     cudaEvent_t e[3];
