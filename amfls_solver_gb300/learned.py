@@ -20,10 +20,18 @@ decisions are randomised (exploration), so that both actions are seen in
 similar states; at run time the controller widens when the predicted rate
 for widening is higher.  The FP64 certificate still decides termination.
 
-    log = collect_decisions(problems, exploration=0.3, seeds=(1, 2))
-    data = dataset(log)
-    policy = WidthPolicy.train(data.inputs, data.targets, epochs=3000)
+    logs = collect_decisions(training_problems, exploration=0.4, exploration_seeds=(1, 2))
+    data = dataset(logs)
+    policy = WidthPolicy.train(data.inputs, data.targets, epochs=2000)
     result, decisions = solve_controlled(matrix, b, policy=policy, tolerance=1e-10)
+    rows = compare_controllers(held_out_problems, policy)
+
+On this GPU the reference's cost gate, which prices local block algebra at
+a CPU's BLAS-3 rates, widens dense solves whose wider levels then run
+slower here (FP64 block reorthogonalisation is bound by the FP64 FMA rate
+and each block level synchronises with the host for its rank decisions);
+the trained policy learns from the measured rates when staying at width one
+finishes sooner.
 """
 from __future__ import annotations
 
@@ -185,3 +193,40 @@ def dataset(logs, scale: float | None = None) -> Dataset:
         scale = float(np.median(np.abs(rate))) or 1.0
     x = np.concatenate([rows[:, :F], rows[:, 11:12]], axis=1)
     return Dataset(x, np.arcsinh(rate / scale), scale)
+
+
+def collect_decisions(problems, *, exploration: float = 0.4, exploration_seeds=(1, 2)):
+    """Decision logs of exploration solves: `problems` yields (matrix or
+    DeviceOperator, b, options dict); each is solved once per exploration
+    seed with that share of its width decisions replaced by a fair coin."""
+    logs = []
+    for matrix, b, options in problems:
+        op = matrix if isinstance(matrix, DeviceOperator) else DeviceOperator(matrix)
+        for es in exploration_seeds:
+            _, log = solve_controlled(op, b, exploration=exploration, exploration_seed=es,
+                                      **options)
+            logs.append(log)
+    return logs
+
+
+def compare_controllers(problems, policy: WidthPolicy):
+    """Time-to-tol of the heuristic and of `policy` on each problem (host
+    wall clock around each synchronous solve, after one untimed warm-up
+    solve of each): rows of (heuristic SolveResult, seconds, learned
+    SolveResult, seconds)."""
+    import time
+
+    rows = []
+    for matrix, b, options in problems:
+        op = matrix if isinstance(matrix, DeviceOperator) else DeviceOperator(matrix)
+        solve_controlled(op, b, **options)
+        solve_controlled(op, b, policy=policy, **options)
+        out = []
+        for pol in (None, policy):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r, _ = solve_controlled(op, b, policy=pol, **options)
+            torch.cuda.synchronize()
+            out += [r, time.perf_counter() - t0]
+        rows.append(tuple(out))
+    return rows

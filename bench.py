@@ -2,7 +2,8 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload NAME] [--c3 0|1] [--dense 0|1] [--spmm 0|1]
-                    [--baselines 0|1] [--batched COUNT] [--cpu-sample 0|1]
+                    [--baselines 0|1] [--learned 0|1] [--batched COUNT]
+                    [--cpu-sample 0|1]
 
 A step is one complete AMFLS solve, to tolerance, of a seeded synthetic
 problem.  The headline workload is the 20000 x 5000 CSR problem (10 nonzeros
@@ -29,6 +30,9 @@ dense     the 100000 x 2000 column-major dense operator (lambda = 1e-6,
           tol = 1e-10): plain FP64 and the mixed form;
 spmm      CSR SpMM / SpMM^T GB/s (s = 1 and 8) on the 2M x 500k matrix;
 baselines AMFLS against scalar LSQR / LSMR on the headline problem;
+learned   the learned width controller against the heuristic: trained on
+          exploration solves of the reference's dense study family, compared
+          by time-to-tol on held-out instances;
 batched   problems/s, p50 / p99 of batched solves of the uneven CSR workload
           (a bounded sample, described in the line);
 cpu_baseline  one complete oracle solve (the CPU restatement of the
@@ -78,6 +82,8 @@ def parse():
                     help="0 skips the CSR SpMM GB/s measurement on the 2M x 500k matrix")
     ap.add_argument("--baselines", type=int, default=1,
                     help="0 skips the AMFLS vs LSQR / LSMR leg")
+    ap.add_argument("--learned", type=int, default=1,
+                    help="0 skips the learned-controller leg on the dense study family")
     ap.add_argument("--batched", type=int, default=48,
                     help="problems in the batched leg's sample (0 skips it)")
     return ap.parse_args()
@@ -385,6 +391,60 @@ def baselines_measurement(dev, op, b, prob, opts):
         return {"error": f"{type(e).__name__}: {e}"}
 
 
+def dense_family(seeds):
+    """The reference's tall dense study cases (16384 x 512, tol 1e-10; the
+    spectral-coverage and ordinary suites, tests/golden/experiment_cases.json)
+    at the given instance seeds, as (case, seed, matrix, b, options)."""
+    from amfls_solver_gb300 import experiments as ex
+
+    cases = json.loads((ROOT / "tests" / "golden" / "experiment_cases.json").read_text())
+    for suite in cases["suites"]:
+        if suite["suite"] not in ("large_dense_spectral_coverage_v1", "large_dense_ordinary_v2"):
+            continue
+        for case in suite["cases"]:
+            for seed in seeds:
+                p = ex.make_problem(case, seed)
+                yield (case["name"], seed, p["matrix"].cuda(), p["b"].cuda(),
+                       dict(regularization=p["regularization"], tolerance=suite["tolerance"],
+                            maximum_epochs=suite["maximum_epochs"],
+                            maximum_depth=suite["maximum_depth"],
+                            maximum_auxiliary_width=suite["maximum_auxiliary_width"],
+                            maximum_basis_size=suite["maximum_basis_size"],
+                            seed=seed + suite["algorithm_seed_offset"]))
+
+
+def learned_measurement(dev):
+    """The learned width controller against the heuristic: trained on
+    exploration solves of the dense study family (instance seeds 201, 202),
+    compared on held-out instances (seeds 101, 102) by time-to-tol."""
+    from amfls_solver_gb300 import learned
+
+    try:
+        t0 = time.perf_counter()
+        train = [(m, b, o) for _, _, m, b, o in dense_family((201, 202))]
+        logs = learned.collect_decisions(train, exploration=0.4, exploration_seeds=(1, 2))
+        data = learned.dataset(logs)
+        policy = learned.WidthPolicy.train(data.inputs, data.targets, epochs=2000)
+        t_train = time.perf_counter() - t0
+        held = list(dense_family((101, 102)))
+        rows = learned.compare_controllers([(m, b, o) for _, _, m, b, o in held], policy)
+        per = []
+        for (name, seed, _, _, _), (h, th, lr, tl) in zip(held, rows):
+            per.append({"case": name, "seed": seed, "heuristic_s": th, "learned_s": tl,
+                        "status": [h.status, lr.status],
+                        "auxiliary_width": [h.auxiliary_width, lr.auxiliary_width],
+                        "operator_columns": [h.a_columns + h.at_columns,
+                                             lr.a_columns + lr.at_columns]})
+        th = sum(r["heuristic_s"] for r in per)
+        tl = sum(r["learned_s"] for r in per)
+        return {"family": "reference dense study, tall cases (16384 x 512), tol 1e-10",
+                "training": {"solves": len(logs), "decisions": int(data.inputs.shape[0]),
+                             "loss": list(policy.losses), "seconds": t_train},
+                "held_out": per, "heuristic_s": th, "learned_s": tl, "gain": 1.0 - tl / th}
+    except Exception as e:  # reported, not fatal to the bench line
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def batched_measurement(dev, count):
     """Batched solves of a bounded sample of the uneven CSR workload."""
     import torch
@@ -553,6 +613,8 @@ def run_ours(args, world, rank, local):
             legs["spmm"] = spmm_measurement(dev, stream, peak)
         if args.dense:
             legs["dense"] = dense_measurement(dev)
+        if args.learned:
+            legs["learned"] = learned_measurement(dev)
         if args.batched > 0:
             legs["batched"] = batched_measurement(dev, args.batched)
         if args.c3:

@@ -19,6 +19,11 @@
  */
 #include "amfls_oracle.h"
 
+/* kind 3 is a CSR matrix behind a custom MatrixOperator: the same products
+ * and model, but no extended-precision validation products (the interface
+ * defaults, matrix_operator.hpp:62-88), so validation never refines. */
+#define IS_CSR(op) ((op)->kind == 0 || (op)->kind == 3)
+
 #include <fenv.h>
 #include <float.h>
 #include <math.h>
@@ -190,7 +195,7 @@ void orc_norm_interval(const double* v, int64_t n, double* lower, double* upper)
 void orc_apply(const orc_operator* op, const double* x, int s, double* y) {
     const int64_t m = op->rows, n = op->cols;
     memset(y, 0, sizeof(double) * (size_t)(m * s));
-    if (op->kind == 0) {
+    if (IS_CSR(op)) {
         for (int64_t r = 0; r < m; ++r)
             for (int64_t e = op->row_offsets[r]; e < op->row_offsets[r + 1]; ++e) {
                 const int64_t c = op->column_indices[e];
@@ -219,7 +224,7 @@ void orc_apply(const orc_operator* op, const double* x, int s, double* y) {
 void orc_apply_transpose(const orc_operator* op, const double* y, int s, double* x) {
     const int64_t m = op->rows, n = op->cols;
     memset(x, 0, sizeof(double) * (size_t)(n * s));
-    if (op->kind == 0) {
+    if (IS_CSR(op)) {
         for (int64_t r = 0; r < m; ++r)
             for (int64_t e = op->row_offsets[r]; e < op->row_offsets[r + 1]; ++e) {
                 const int64_t c = op->column_indices[e];
@@ -249,7 +254,7 @@ void orc_apply_transpose(const orc_operator* op, const double* y, int s, double*
  * stored binary64 entries (row sums for A, row-ordered scatter for A^T). */
 static int apply_ld(const orc_operator* op, const long double* x, long double* y) {
     const int64_t m = op->rows, n = op->cols;
-    if (op->kind == 0) {
+    if (IS_CSR(op)) {
         for (int64_t r = 0; r < m; ++r) {
             long double acc = 0.0L;
             for (int64_t e = op->row_offsets[r]; e < op->row_offsets[r + 1]; ++e)
@@ -293,7 +298,7 @@ static int apply_transpose_ld(const orc_operator* op, const long double* y, long
     for (int64_t r = 0; r < m; ++r) {
         const long double yr = y[r];
         if (!isfinite(yr)) return 0;
-        if (op->kind == 0) {
+        if (IS_CSR(op)) {
             for (int64_t e = op->row_offsets[r]; e < op->row_offsets[r + 1]; ++e)
                 x[op->column_indices[e]] += (long double)op->values[e] * yr;
         } else {
@@ -314,7 +319,7 @@ int orc_model_of(const orc_operator* op, orc_model* out) {
     double max_row_sum = 0.0, max_col_sum = 0.0, max_two_lower = 0.0, max_entry = 0.0;
     double frob2 = 0.0;
     int certifiable = 1;
-    if (op->kind == 0) {
+    if (IS_CSR(op)) {
         int64_t max_row_nnz = 0, max_col_nnz = 0;
         int64_t* col_nnz = calloc((size_t)n, sizeof(int64_t));
         double* col_sum = calloc((size_t)n, sizeof(double));
@@ -922,7 +927,8 @@ void orc_validate(const orc_operator* op, const orc_model* mdl, const double* b,
         envelope e = base_envelope(mdl, b, x, ax, res, atr, g, m, n, reg);
         r->operator_norm_lower_bound = e.op_lower;
         certified_contract(r, &e, reg, tol, 0, 0.0);
-        if (r->status != ST_SUCCESS && e.certified && e.grad_radius >= r->normal_residual_norm) {
+        if (op->kind != 3 && r->status != ST_SUCCESS && e.certified &&
+            e.grad_radius >= r->normal_residual_norm) {
             envelope e2;
             if (refine(op, mdl, b, x, reg, ax, res, atr, g, &e2, r)) {
                 e = e2;

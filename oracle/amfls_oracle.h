@@ -8,7 +8,8 @@
 #include <stdint.h>
 
 /* Operator description: kind 0 = CSR (int64 offsets / indices), 1 = row-major
- * dense, 2 = column-major dense. */
+ * dense, 2 = column-major dense, 3 = CSR behind a custom MatrixOperator (no
+ * extended-precision validation products). */
 typedef struct {
     int kind;
     int rows;

@@ -117,15 +117,18 @@ class Operator:
     """CSR or dense operator with the reference's MatrixOperator contract
     (include/amfls/matrix_operator.hpp:29-89)."""
 
-    def __init__(self, problem):
+    def __init__(self, problem, custom=False):
+        """custom=True puts a CSR matrix behind a custom MatrixOperator: the
+        same products and model but no extended-precision validation
+        products (the interface defaults, matrix_operator.hpp:62-88)."""
         if hasattr(problem, "row_offsets"):
-            self.kind = 0
+            self.kind = 3 if custom else 0
             self._keep = [np.ascontiguousarray(problem.row_offsets, dtype=np.int64),
                           np.ascontiguousarray(problem.column_indices, dtype=np.int64),
                           np.ascontiguousarray(problem.values, dtype=np.float64)]
             off, col, val = self._keep
             self.rows, self.cols = int(problem.rows), int(problem.cols)
-            self._spec = _OrcOperator(0, self.rows, self.cols, off.ctypes.data,
+            self._spec = _OrcOperator(self.kind, self.rows, self.cols, off.ctypes.data,
                                       col.ctypes.data, val.ctypes.data, val.shape[0])
         else:
             a = problem.matrix
@@ -146,7 +149,7 @@ class Operator:
         # operators charge one shared pass (dense_operator.cpp:100-105).
         if block_cols <= 0:
             return INF
-        return float(block_cols) if self.kind == 0 else 1.0
+        return float(block_cols) if self.kind in (0, 3) else 1.0
 
     def model(self):
         m = self._model
@@ -168,7 +171,7 @@ class Operator:
         return sblas.dgemm(1.0, at, v, trans_a=0 if transpose else 1)
 
     def apply(self, x):
-        if self.kind != 0:
+        if self.kind not in (0, 3):
             return self._dense_product(np.asarray(x, dtype=np.float64), False)
         x = np.asfortranarray(x, dtype=np.float64)
         s = 1 if x.ndim == 1 else x.shape[1]
@@ -177,7 +180,7 @@ class Operator:
         return y
 
     def apply_transpose(self, y):
-        if self.kind != 0:
+        if self.kind not in (0, 3):
             return self._dense_product(np.asarray(y, dtype=np.float64), True)
         y = np.asfortranarray(y, dtype=np.float64)
         s = 1 if y.ndim == 1 else y.shape[1]
@@ -1073,9 +1076,11 @@ def _certificate(r, reg):
 
 def solve_amfls(problem, regularization=0.0, tolerance=1e-8, failure_probability=1e-6,
                 maximum_epochs=0, maximum_depth=0, maximum_auxiliary_width=0,
-                maximum_basis_size=0, seed=0, stream=0, replay=None):
-    """amfls.cpp:57-661. Returns the result dict in the torch binding's layout."""
-    op = Operator(problem)
+                maximum_basis_size=0, seed=0, stream=0, replay=None, custom=False):
+    """amfls.cpp:57-661. Returns the result dict in the torch binding's layout.
+    custom=True solves a CSR problem through a custom MatrixOperator (see
+    Operator)."""
+    op = Operator(problem, custom=custom)
     b = np.ascontiguousarray(problem.b, dtype=np.float64)
     return solve_amfls_operator(op, b, regularization, tolerance, failure_probability,
                                 maximum_epochs, maximum_depth, maximum_auxiliary_width,

@@ -50,13 +50,15 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
-def _operator_args(problem):
-    """(kind, rows, cols, offsets, indices, values, nnz, keep-alive list)."""
+def _operator_args(problem, custom=False):
+    """(kind, rows, cols, offsets, indices, values, nnz, keep-alive list);
+    custom=True puts a CSR matrix behind a custom MatrixOperator (kind 3)."""
     if hasattr(problem, "row_offsets"):
         off = np.ascontiguousarray(problem.row_offsets, dtype=np.int64)
         col = np.ascontiguousarray(problem.column_indices, dtype=np.int64)
         val = np.ascontiguousarray(problem.values, dtype=np.float64)
-        return 0, problem.rows, problem.cols, off, col, val, val.shape[0], [off, col, val]
+        return (3 if custom else 0), problem.rows, problem.cols, off, col, val, val.shape[0], \
+            [off, col, val]
     a = problem.matrix
     if a.flags.c_contiguous:
         return 1, a.shape[0], a.shape[1], None, None, a, a.size, [a]
@@ -75,7 +77,8 @@ _ALGORITHMS = {"amfls": 0, "fixed_rbgk": 1, "lsqr": 2, "lsmr": 3}
 def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
           failure_probability=1e-6, maximum_epochs=0, maximum_depth=0,
           maximum_auxiliary_width=0, maximum_basis_size=0, seed=0, stream=0,
-          auxiliary_width=4, maximum_iterations=0, trace_capacity=4096, replay=None):
+          auxiliary_width=4, maximum_iterations=0, trace_capacity=4096, replay=None,
+          custom=False):
     """algorithm: amfls, fixed_rbgk, lsqr or lsmr (the last two take
     regularization, tolerance and maximum_iterations only).
 
@@ -84,10 +87,12 @@ def solve(problem, *, algorithm="amfls", regularization=0.0, tolerance=1e-8,
     matched horizons) and ``replay_overrun``.  ``replay`` (a sequence of 0/1)
     makes the controller take those decisions in order instead of its
     timing-driven ones (sites beyond the list keep the reference's choice and
-    are counted in ``replay_overrun``)."""
+    are counted in ``replay_overrun``).  custom=True solves through a custom
+    MatrixOperator over the CSR matrix (no extended-precision validation
+    products)."""
     if algorithm in ("lsqr", "lsmr"):
         maximum_depth = maximum_iterations
-    kind, m, n, off, col, val, nnz, keep = _operator_args(problem)
+    kind, m, n, off, col, val, nnz, keep = _operator_args(problem, custom)
     b = np.ascontiguousarray(problem.b, dtype=np.float64)
     x = np.zeros(n)
     metrics = np.zeros(21)

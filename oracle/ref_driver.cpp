@@ -66,7 +66,7 @@ amfls::detail::WidthDecision amfls::detail::ref_hook_width_decision(WidthDecisio
 namespace {
 
 struct OperatorSpec {
-    int kind;  // 0 CSR, 1 row-major dense, 2 column-major dense
+    int kind;  // 0 CSR, 1 row-major dense, 2 column-major dense, 3 CSR behind a custom operator
     int rows;
     int cols;
     const std::int64_t* row_offsets;
@@ -75,8 +75,36 @@ struct OperatorSpec {
     std::int64_t nonzeros;
 };
 
+// A user's custom MatrixOperator over a CSR matrix: it forwards the products
+// and the validation error model of a SparseCsrOperator and keeps the
+// interface defaults for everything else (block cost, no extended-precision
+// validation products, matrix_operator.hpp:45-88).
+class ForwardingOperator final : public amfls::MatrixOperator {
+public:
+    explicit ForwardingOperator(std::unique_ptr<amfls::MatrixOperator> inner)
+        : inner_(std::move(inner)) {}
+    int rows() const override { return inner_->rows(); }
+    int cols() const override { return inner_->cols(); }
+    void apply(const double* x, int block_cols, double* y) const override {
+        inner_->apply(x, block_cols, y);
+    }
+    void apply_transpose(const double* y, int block_cols, double* x) const override {
+        inner_->apply_transpose(y, block_cols, x);
+    }
+    amfls::MatrixOperatorValidationErrorModel validation_error_model() const noexcept override {
+        return inner_->validation_error_model();
+    }
+
+private:
+    std::unique_ptr<amfls::MatrixOperator> inner_;
+};
+
 std::unique_ptr<amfls::MatrixOperator> make_operator(const OperatorSpec& s) {
     using namespace amfls::math;
+    if (s.kind == 3) {
+        return std::make_unique<ForwardingOperator>(std::make_unique<SparseCsrOperator>(
+            s.rows, s.cols, s.row_offsets, s.column_indices, s.values, s.nonzeros));
+    }
     if (s.kind == 0) {
         return std::make_unique<SparseCsrOperator>(
             s.rows, s.cols, s.row_offsets, s.column_indices, s.values,

@@ -78,6 +78,7 @@ def load_replay(name):
 
 SOLVE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("solve_*.npz"))
 REPLAY_FIXTURES = sorted(p.stem for p in GOLDEN.glob("replay_*.npz"))
+CUSTOM_FIXTURES = sorted(p.stem for p in GOLDEN.glob("custom_*.npz"))
 BASELINE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("baseline_*.npz"))
 
 

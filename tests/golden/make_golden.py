@@ -141,6 +141,27 @@ def replay_fixture(name, generator, store=False, **opts):
           f"widenings {c[34]} decisions {''.join(map(str, r['decisions']))}")
 
 
+def customs():
+    """CSR problems of the solve fixtures solved through a custom
+    MatrixOperator (the reference driver's forwarding operator: products and
+    validation model of the CSR matrix, no extended-precision validation
+    products), the counterpart of a callback operator."""
+    c1 = problems.scaled_uniform_csr(2000, 500, seed=1)
+    c2 = problems.power_law_csr(3000, 800, decades=4.0, noise=1e-6, seed=4)
+    c3 = problems.scaled_uniform_csr(600, 1500, per_row=12, decades=3.0, noise=1e-3, seed=9)
+    c4 = problems.scaled_uniform_csr(1500, 200, per_row=6, decades=2.0, noise=1.0, seed=21)
+    solve_fixture("custom_csr_ls", c1, csr_arrays(c1), custom=True, regularization=0.0,
+                  tolerance=1e-8, seed=7)
+    solve_fixture("custom_csr_ridge", c1, csr_arrays(c1), custom=True, regularization=1e-4,
+                  tolerance=1e-10, seed=7)
+    solve_fixture("custom_powerlaw_ridge", c2, csr_arrays(c2), custom=True, regularization=1e-4,
+                  tolerance=1e-10)
+    solve_fixture("custom_csr_wide", c3, csr_arrays(c3), custom=True, regularization=0.0,
+                  tolerance=1e-8)
+    solve_fixture("custom_csr_inconsistent", c4, csr_arrays(c4), custom=True,
+                  regularization=0.0, tolerance=1e-13)
+
+
 def replays():
     """The 20000 x 5000 CSR workload (bench seed; arrays stored) and widening
     solves on portable problems."""
@@ -288,12 +309,16 @@ def baselines():
 
 if __name__ == "__main__":
     # no argument: every fixture; "baselines": only the LSQR / LSMR ones;
-    # "replays": only the schedule-replay fixtures
+    # "replays": only the schedule-replay fixtures; "customs": only the
+    # custom-operator ones
     if sys.argv[1:] == ["baselines"]:
         baselines()
     elif sys.argv[1:] == ["replays"]:
         replays()
+    elif sys.argv[1:] == ["customs"]:
+        customs()
     else:
         main()
         baselines()
         replays()
+        customs()

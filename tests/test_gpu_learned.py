@@ -2,9 +2,10 @@
 reference): the CUDA forward pass and gradient against the numpy oracle
 (oracle/width_mlp.py, itself pinned by finite differences), deterministic
 GPU training, the controlled solve without a policy equal to the
-reference's controller, and a trained policy on held-out problems, whose
-gain over the heuristic is measured and printed (the FP64 certificate still
-decides termination, so every solve must certify as the heuristic's does)."""
+reference's controller, and a policy trained on the dense study family that
+must beat the heuristic's time-to-tol on held-out instances by at least 20%
+(the FP64 certificate still decides termination, so every solve must end
+with the heuristic's status)."""
 import numpy as np
 import pytest
 import torch
@@ -71,37 +72,53 @@ def test_uncontrolled_solve_is_the_reference_controller(mods):
         assert np.array_equal(log[:, 11], log[:, 12])  # every action is the heuristic's
 
 
-def test_trained_policy_on_held_out_problems(mods):
-    amfls, learned = mods
-    from amfls_solver_gb300 import problems
+def _dense_family(seeds, suites=("large_dense_spectral_coverage_v1", "large_dense_ordinary_v2")):
+    """The reference's tall dense study cases (16384 x 512, lambda = 0,
+    tol 1e-10: flat, clustered, polynomial, exponential-tail, outlier and
+    smooth-tail spectra) at the given instance seeds, as (matrix, b,
+    options) for the learned controller's helpers."""
+    import json
+    from conftest import GOLDEN
+    from amfls_solver_gb300 import experiments as ex
 
-    opts = dict(tolerance=1e-10, maximum_auxiliary_width=64)
-    logs = []
-    for i, m in enumerate([4000, 6000, 8000]):
-        prob = problems.banded_random_csr(m, m // 4, decades=9.0, seed=200 + i)
-        op = amfls.DeviceOperator(csr_tensor(prob))
-        b = torch.from_numpy(prob.b).cuda()
-        for reg in (0.0, 1e-6):
-            for es in (1, 2):
-                r, log = learned.solve_controlled(op, b, exploration=0.4, exploration_seed=es + 7 * i,
-                                                  regularization=reg, **opts)
-                logs.append(log)
+    cases = json.loads((GOLDEN / "experiment_cases.json").read_text())
+    for suite in cases["suites"]:
+        if suite["suite"] not in suites:
+            continue
+        for case in suite["cases"]:
+            for seed in seeds:
+                p = ex.make_problem(case, seed)
+                yield (p["matrix"].cuda(), p["b"].cuda(),
+                       dict(regularization=p["regularization"], tolerance=suite["tolerance"],
+                            maximum_epochs=suite["maximum_epochs"],
+                            maximum_depth=suite["maximum_depth"],
+                            maximum_auxiliary_width=suite["maximum_auxiliary_width"],
+                            maximum_basis_size=suite["maximum_basis_size"],
+                            seed=seed + suite["algorithm_seed_offset"]))
+
+
+def test_trained_policy_gains_on_held_out_problems(mods):
+    """The network trained on exploration solves of the dense study family
+    (instance seeds 201, 202) against the heuristic on held-out instances
+    (seed 101): the same status on every problem, certified results within
+    tol, and at least 20% less total time-to-tol.  On this GPU the
+    heuristic's cost gate widens the exponential- and smooth-tail solves,
+    whose block levels then run slower than width-one levels; the policy
+    learns from the measured rates to stay."""
+    amfls, learned = mods
+    logs = learned.collect_decisions(list(_dense_family((201, 202))), exploration=0.4,
+                                     exploration_seeds=(1, 2))
     data = learned.dataset(logs)
     policy = learned.WidthPolicy.train(data.inputs, data.targets, epochs=2000)
     assert policy.losses[1] < policy.losses[0]
-    work = {"heuristic": 0, "learned": 0}
-    for i, m in enumerate([10000, 12000]):
-        prob = problems.banded_random_csr(m, m // 4, decades=9.0, seed=900 + i)
-        op = amfls.DeviceOperator(csr_tensor(prob))
-        b = torch.from_numpy(prob.b).cuda()
-        for reg in (0.0, 1e-6):
-            h, _ = learned.solve_controlled(op, b, regularization=reg, **opts)
-            lr, log = learned.solve_controlled(op, b, policy=policy, regularization=reg, **opts)
-            assert lr.status == h.status  # the certificate judges both the same way
-            if lr.status == 0:
-                assert (lr.backward_error_upper_bound if reg == 0.0
-                        else lr.relative_energy_error_upper_bound) <= 1e-10
-            work["heuristic"] += h.a_columns + h.at_columns
-            work["learned"] += lr.a_columns + lr.at_columns
-    print(f"\noperator columns on held-out problems: heuristic {work['heuristic']}, "
-          f"learned {work['learned']} (gain {1 - work['learned'] / work['heuristic']:+.1%})")
+    rows = learned.compare_controllers(list(_dense_family((101,))), policy)
+    t_h = t_l = 0.0
+    for h, th, lr, tl in rows:
+        assert lr.status == h.status  # the certificate judges both the same way
+        if lr.status == 0:
+            assert lr.backward_error_upper_bound <= 1e-10
+        t_h += th
+        t_l += tl
+    print(f"\ntime-to-tol on {len(rows)} held-out problems: heuristic {t_h:.3f} s, "
+          f"learned {t_l:.3f} s (gain {1 - t_l / t_h:+.1%})")
+    assert t_l <= 0.8 * t_h

@@ -9,7 +9,7 @@ relative tolerances.
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, SOLVE_FIXTURES, golden_options, load_golden
+from conftest import CUSTOM_FIXTURES, GOLDEN, SOLVE_FIXTURES, golden_options, load_golden
 from oracle import amfls_oracle as orc
 
 ULP_TOL = 1e-14
@@ -89,3 +89,18 @@ def test_oracle_solve_matches_reference(name):
             assert abs(a - b) <= rel * abs(b) + 1e-13, (idx, a, b)
         else:
             assert a == b
+
+
+@pytest.mark.parametrize("name", CUSTOM_FIXTURES)
+def test_oracle_custom_operator_solve_matches_reference(name):
+    """A CSR matrix behind a custom MatrixOperator (the reference driver's
+    forwarding operator: no extended-precision validation products,
+    matrix_operator.hpp:62-88): the oracle's kind-3 operator reproduces the
+    reference's counters, trace and solution."""
+    data, prob = load_golden(name)
+    r = orc.solve_amfls(prob, custom=True, **golden_options(data))
+    assert (r["status"], r["stop_reason"]) == (int(data["status"]), int(data["stop_reason"]))
+    np.testing.assert_array_equal(r["counters"], data["counters"])
+    np.testing.assert_array_equal(r["trace_int"], data["trace_int"])
+    xr = data["solution"]
+    assert np.linalg.norm(r["solution"] - xr) <= 1e-9 * max(np.linalg.norm(xr), 1e-300)
