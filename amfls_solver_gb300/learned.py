@@ -13,15 +13,23 @@ the two choices at each such decision from the controller's own features:
   4 log10 block-cost ratio            10 the heuristic's own choice
   5 log2(1 + current width)
 
-plus the action (0 stay, 1 widen).  Its target is the rate at which the
-certificate fell over the interval after the decision (decades per second),
-compressed as asinh(rate / scale).  Training data come from solves whose
-decisions are randomised (exploration), so that both actions are seen in
-similar states; at run time the controller widens when the predicted rate
-for widening is higher.  The FP64 certificate still decides termination.
+plus the action (0 stay, 1 widen), and predicts how good that action is;
+at run time the controller widens when the score for widening is higher,
+and the FP64 certificate still decides termination.  Two training sources:
 
-    logs = collect_decisions(training_problems, exploration=0.4, exploration_seeds=(1, 2))
-    data = dataset(logs)
+* counterfactual_dataset: the plain controller's own traces.  At each of
+  the heuristic's decision sites the solve is replayed with the opposite
+  choice (schedule replay) and timed; the target is the log speed-up of an
+  action over the heuristic's (0 for the heuristic's own).  Both actions are
+  seen in exactly the same state, so the score is not confounded by when
+  decisions happen.
+* dataset(collect_decisions(...)): exploration solves whose decisions are
+  randomised; the target is the rate at which the certificate fell after
+  the decision (decades per second, compressed as asinh(rate / scale)).
+  Early decisions see fast certificate decay whatever the action, so this
+  target mixes the state into the action's value.
+
+    data = counterfactual_dataset(training_problems)   # or dataset(collect_decisions(...))
     policy = WidthPolicy.train(data.inputs, data.targets, epochs=2000)
     result, decisions = solve_controlled(matrix, b, policy=policy, tolerance=1e-10)
     rows = compare_controllers(held_out_problems, policy)
@@ -207,6 +215,48 @@ def collect_decisions(problems, *, exploration: float = 0.4, exploration_seeds=(
                                       **options)
             logs.append(log)
     return logs
+
+
+def counterfactual_dataset(problems, *, max_sites: int = 8) -> Dataset:
+    """Training pairs from the plain controller's own traces, without the
+    confounding of random exploration: for each problem the heuristic solve
+    is logged (its features at every decision site) and timed; then, for
+    each of its first `max_sites` decision sites, the solve is replayed with
+    the heuristic's bits up to that site and the opposite bit there
+    (amfls_gpu_solve_amfls_replay; later sites follow the heuristic again)
+    and timed.  The site's features with the heuristic's action get target
+    0, with the opposite action log(t_heuristic / t_flipped): the log
+    speed-up that choice would have brought.  A policy trained on these
+    scores picks, at each site, the action predicted to finish sooner."""
+    import time
+
+    from .binding import solve_amfls_replay
+
+    xs, ys = [], []
+    for matrix, b, options in problems:
+        op = matrix if isinstance(matrix, DeviceOperator) else DeviceOperator(matrix)
+        solve_controlled(op, b, **options)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, log = solve_controlled(op, b, **options)
+        torch.cuda.synchronize()
+        t_h = time.perf_counter() - t0
+        bits = [int(v) for v in log[:, 11]] if len(log) else []
+        for i in range(min(len(bits), max_sites)):
+            replay = bits[:i] + [1 - bits[i]]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            solve_amfls_replay(op, b, replay, **options)
+            torch.cuda.synchronize()
+            t_f = time.perf_counter() - t0
+            f = log[i, :F]
+            xs.append(np.concatenate([f, [bits[i]]]))
+            ys.append(0.0)
+            xs.append(np.concatenate([f, [1 - bits[i]]]))
+            ys.append(float(np.log(t_h / t_f)))
+    if not xs:
+        raise ValueError("no decision site in the training problems")
+    return Dataset(np.asarray(xs), np.asarray(ys), 1.0)
 
 
 def compare_controllers(problems, policy: WidthPolicy):

@@ -414,16 +414,16 @@ def dense_family(seeds):
 
 
 def learned_measurement(dev):
-    """The learned width controller against the heuristic: trained on
-    exploration solves of the dense study family (instance seeds 201, 202),
-    compared on held-out instances (seeds 101, 102) by time-to-tol."""
+    """The learned width controller against the heuristic: trained on the
+    plain controller's counterfactual traces of the dense study family
+    (instance seeds 201, 202), compared on held-out instances (seeds 101,
+    102) by time-to-tol."""
     from amfls_solver_gb300 import learned
 
     try:
         t0 = time.perf_counter()
         train = [(m, b, o) for _, _, m, b, o in dense_family((201, 202))]
-        logs = learned.collect_decisions(train, exploration=0.4, exploration_seeds=(1, 2))
-        data = learned.dataset(logs)
+        data = learned.counterfactual_dataset(train, max_sites=8)
         policy = learned.WidthPolicy.train(data.inputs, data.targets, epochs=2000)
         t_train = time.perf_counter() - t0
         held = list(dense_family((101, 102)))
@@ -438,7 +438,7 @@ def learned_measurement(dev):
         th = sum(r["heuristic_s"] for r in per)
         tl = sum(r["learned_s"] for r in per)
         return {"family": "reference dense study, tall cases (16384 x 512), tol 1e-10",
-                "training": {"solves": len(logs), "decisions": int(data.inputs.shape[0]),
+                "training": {"problems": len(train), "pairs": int(data.inputs.shape[0]),
                              "loss": list(policy.losses), "seconds": t_train},
                 "held_out": per, "heuristic_s": th, "learned_s": tl, "gain": 1.0 - tl / th}
     except Exception as e:  # reported, not fatal to the bench line

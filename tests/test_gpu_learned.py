@@ -2,8 +2,8 @@
 reference): the CUDA forward pass and gradient against the numpy oracle
 (oracle/width_mlp.py, itself pinned by finite differences), deterministic
 GPU training, the controlled solve without a policy equal to the
-reference's controller, and a policy trained on the dense study family that
-must beat the heuristic's time-to-tol on held-out instances by at least 20%
+reference's controller, and a policy trained on counterfactual traces of the
+dense study family that must beat the heuristic's time-to-tol on held-out instances by at least 20%
 (the FP64 certificate still decides termination, so every solve must end
 with the heuristic's status)."""
 import numpy as np
@@ -98,17 +98,16 @@ def _dense_family(seeds, suites=("large_dense_spectral_coverage_v1", "large_dens
 
 
 def test_trained_policy_gains_on_held_out_problems(mods):
-    """The network trained on exploration solves of the dense study family
-    (instance seeds 201, 202) against the heuristic on held-out instances
-    (seed 101): the same status on every problem, certified results within
-    tol, and at least 20% less total time-to-tol.  On this GPU the
-    heuristic's cost gate widens the exponential- and smooth-tail solves,
-    whose block levels then run slower than width-one levels; the policy
-    learns from the measured rates to stay."""
+    """The network trained on the plain controller's counterfactual traces
+    of the dense study family (instance seed 201: every decision site
+    replayed with the other choice and timed) against the heuristic on
+    held-out instances (seed 101): the same status on every problem,
+    certified results within tol, and at least 20% less total time-to-tol.
+    On this GPU the heuristic's cost gate widens the exponential- and
+    smooth-tail solves, whose block levels then run slower than width-one
+    levels; the traces teach the policy to stay."""
     amfls, learned = mods
-    logs = learned.collect_decisions(list(_dense_family((201, 202))), exploration=0.4,
-                                     exploration_seeds=(1, 2))
-    data = learned.dataset(logs)
+    data = learned.counterfactual_dataset(list(_dense_family((201,))), max_sites=8)
     policy = learned.WidthPolicy.train(data.inputs, data.targets, epochs=2000)
     assert policy.losses[1] < policy.losses[0]
     rows = learned.compare_controllers(list(_dense_family((101,))), policy)
