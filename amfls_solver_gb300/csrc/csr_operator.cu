@@ -318,16 +318,7 @@ void make_tiles(const std::vector<long long>& off, int count, int E, int C, bool
         std::nth_element(lens.begin(), lens.begin() + count / 2, lens.end());
         chains = lens[count / 2] <= kChainShort;
     }
-    // single-column row blocks of a small side hold at most kSeqMax elements
-    // (every row a sequential chain): such a side has too few 256-element
-    // tiles to give every SM several warps, and a product lasts as long as
-    // its slowest warp.  AMFLS_GB300_CSR_SMALL_TILES=0 keeps E.
-    long long cap = E;
-    if (!chains && C == 1 && count > 0 && off[count] < kChainMinNonzeros) {
-        const char* small = std::getenv("AMFLS_GB300_CSR_SMALL_TILES");
-        if (!(small && std::string(small) == "0")) cap = kSeqMax;
-    }
-    const long long longer_than = chains ? kChainMax : cap;
+    const long long longer_than = chains ? kChainMax : E;
     const long long task = (long long)kRowTaskTiles * E;
     for (int r = 0; r < count; ++r) {
         const long long len = length(r);
@@ -403,7 +394,7 @@ void make_tiles(const std::vector<long long>& off, int count, int E, int C, bool
             }
             const int r0 = r;
             const long long e0 = off[r];
-            while (r < count && length(r) <= longer_than && off[r + 1] - e0 <= cap && r - r0 < cap)
+            while (r < count && length(r) <= longer_than && off[r + 1] - e0 <= E && r - r0 < E)
                 ++r;
             tiles.push_back(make_int4(r0, r, (int)e0, (int)off[r]));
             split.push_back(kRowBlock);

@@ -24,6 +24,7 @@
 // checkpoint is enqueued without a host round trip.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <stdexcept>
@@ -83,6 +84,15 @@ constexpr int kMaxGemvTargetBlocks = 16 * 256;
 // v_c_kernel, which run closest to the FP64 roof there; shorter ones use the
 // warp-task sweeps, whose grid does not shrink with n.
 constexpr int kWarpSweepMaxRows = 1 << 17;
+
+// Which sweeps a basis of n rows uses; AMFLS_GB300_WARP_SWEEPS=0 / 1 in the
+// environment forces the block / warp-task kernels (for measurements).
+bool use_warp_sweeps(long long n) {
+    const char* v = std::getenv("AMFLS_GB300_WARP_SWEEPS");
+    if (v && v[0] == '0') return false;
+    if (v && v[0] == '1') return true;
+    return n < kWarpSweepMaxRows;
+}
 
 enum Hook { kHookNone = 0, kHookRightPass1 = 1, kHookRightPass2 = 2 };
 
@@ -897,6 +907,7 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     const long long pcount = vc_partials_offset_ + (n_ + 31) / 32 + 1024;
     stream_alloc(&partials_, sizeof(double) * pcount, stream_);
     sweep_grid_ = sweep_grid();
+    warp_sweeps_ = use_warp_sweeps(n_);
     sweep_panels_ = max_panels;
     const long long tiles = (n_ + 31) / 32;
     stream_alloc(&sweep_part_, sizeof(double) * sweep_part_doubles(n_, max_panels, sweep_grid_),
@@ -1078,7 +1089,7 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     for (int pass = 1; pass <= 2; ++pass) {
         double* c = pass == 1 ? c1_ : c2_;
         const int hook = pass == 1 ? kHookRightPass1 : kHookRightPass2;
-        if (n_ < kWarpSweepMaxRows) {
+        if (warp_sweeps_) {
             sweep_vt_kernel<<<sweep_grid_, kThreads, 0, s>>>(V_->device_table(), n_, R_, c,
                                                              sweep_part_, panel_tickets, dstate_,
                                                              pass);
@@ -1294,7 +1305,7 @@ void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double se
     AMFLS_CUDA(cudaMemcpyAsync(st, &h, sizeof(DevState), cudaMemcpyHostToDevice, s));
     probe_fill_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), n, k, r);
     AMFLS_LAUNCHED();
-    const bool warp_sweeps = n < kWarpSweepMaxRows;  // as enqueue_level_kernels chooses
+    const bool warp_sweeps = use_warp_sweeps(n);  // as the workspace chooses
     int pcap = 4;
     while (pcap < P) pcap *= 2;
     const int max_chunks = (int)std::max<long long>(1, (n + 255) / 256);

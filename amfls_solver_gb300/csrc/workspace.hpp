@@ -156,6 +156,7 @@ private:
     // basis sweeps (sweep_vt_kernel / sweep_vc_kernel): their grid, partial
     // sums, per-tile sums of squares and tickets (panels | tiles | done)
     int sweep_grid_ = 0;
+    bool warp_sweeps_ = true;
     double* sweep_part_ = nullptr;
     double* sweep_sq_ = nullptr;
     unsigned* sweep_tickets_ = nullptr;

@@ -470,6 +470,16 @@ def batched_measurement(dev, count):
                 "problems_per_s": count / wall, "wall_s": wall,
                 "p50_s": float(np.percentile(secs, 50)), "p99_s": float(np.percentile(secs, 99)),
                 "certified": st.count(0), "levels": int(sum(r.depth for r in res))}
+        # FP64 FMA floor of the batch: basis sweeps (one V^T r and one r - V c
+        # per level: n k FMAs each at basis size k) and the two products per
+        # level, at two FP64 lanes per SM clock
+        fmas = sum(p.cols * r.basis_rank ** 2 + 2.0 * p.nnz * r.depth
+                   for (p, _, _), r in zip(batch, res))
+        props = torch.cuda.get_device_properties(dev)
+        rate = 2.0 * props.multi_processor_count * 2.07e9
+        out["fp64_fma_floor_s"] = fmas / rate
+        out["fp64_fma_floor_note"] = ("sum over problems of n k^2 + 2 nnz depth FMAs at "
+                                      f"{rate / 1e12:.2f} T FMA/s (2 FP64 lanes per SM clock)")
         return out
     except Exception as e:
         return {"error": f"{type(e).__name__}: {e}"}

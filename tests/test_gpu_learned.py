@@ -99,15 +99,15 @@ def _dense_family(seeds, suites=("large_dense_spectral_coverage_v1", "large_dens
 
 def test_trained_policy_gains_on_held_out_problems(mods):
     """The network trained on the plain controller's counterfactual traces
-    of the dense study family (instance seed 201: every decision site
-    replayed with the other choice and timed) against the heuristic on
+    of the dense study family (instance seeds 201 and 202: every decision
+    site replayed with the other choice and timed) against the heuristic on
     held-out instances (seed 101): the same status on every problem,
     certified results within tol, and at least 20% less total time-to-tol.
     On this GPU the heuristic's cost gate widens the exponential- and
     smooth-tail solves, whose block levels then run slower than width-one
     levels; the traces teach the policy to stay."""
     amfls, learned = mods
-    data = learned.counterfactual_dataset(list(_dense_family((201,))), max_sites=8)
+    data = learned.counterfactual_dataset(list(_dense_family((201, 202))), max_sites=8)
     policy = learned.WidthPolicy.train(data.inputs, data.targets, epochs=2000)
     assert policy.losses[1] < policy.losses[0]
     rows = learned.compare_controllers(list(_dense_family((101,))), policy)
