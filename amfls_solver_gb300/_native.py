@@ -75,7 +75,7 @@ EXPORTED = [
     "amfls_gpu_solve_amfls_controlled", "amfls_gpu_solve_amfls_batch",
     "amfls_gpu_callback_operator_create", "amfls_gpu_default_baseline_options",
     "amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr", "amfls_gpu_solve_amfls_replay",
-    "amfls_gpu_probe_reorthogonalization",
+    "amfls_gpu_probe_reorthogonalization", "amfls_gpu_csr_operator_schedule",
 ]
 
 POLICY_FEATURES = 11
@@ -147,6 +147,7 @@ def load():
     lib.amfls_gpu_solve_amfls_replay.argtypes = [P, P, ctypes.POINTER(Options), P, I, P, I, P,
                                                  P, P, ctypes.POINTER(Result), P, P, I, P]
     lib.amfls_gpu_probe_reorthogonalization.argtypes = [I, I, I, P, P]
+    lib.amfls_gpu_csr_operator_schedule.argtypes = [P, P, P]
     _lib = lib
     return lib
 

@@ -232,10 +232,19 @@ class DeviceOperator:
                                             "strides": (8, 8 * nrows)}
             return torch.as_tensor(_Block(), device=dev)
 
+        def solver_stream(handle):
+            # the solver's stream as a torch stream: a NULL handle is the
+            # legacy default stream, which is torch's default stream (an
+            # ExternalStream over 0 would be a different stream, unordered
+            # with the solver's kernels)
+            if not handle:
+                return torch.cuda.default_stream(dev)
+            return torch.cuda.ExternalStream(handle, device=dev)
+
         def wrap(fn, in_rows, out_rows):
             def call(_ctx, src, s, dst, stream):
                 try:
-                    with torch.cuda.stream(torch.cuda.ExternalStream(stream or 0, device=dev)):
+                    with torch.cuda.stream(solver_stream(stream)):
                         fn(view(src, in_rows, s), view(dst, out_rows, s))
                     return 0
                 except Exception:  # reported to the solver as a failed product
@@ -290,6 +299,19 @@ class DeviceOperator:
         _native.check(fn(self.handle, xc.data_ptr(), s, yc.data_ptr(), _stream_handle(x.device)))
         y = yc.t()
         return y.reshape(-1) if vec else y
+
+    def tile_schedule(self):
+        """CSR operators: ({"A": "chains" | "row blocks", "A^T": ...}, timings
+        in microseconds {(side, tiling): us} of the construction-time
+        autotuner, empty where it did not run)."""
+        chains = (ctypes.c_int * 2)()
+        us = (ctypes.c_double * 4)()
+        _native.check(_native.load().amfls_gpu_csr_operator_schedule(self.handle, chains, us))
+        names = ("A", "A^T")
+        choice = {names[i]: "chains" if chains[i] else "row blocks" for i in range(2)}
+        times = {f"{names[i // 2]} {'chains' if i % 2 else 'row blocks'}": us[i]
+                 for i in range(4) if us[i] > 0}
+        return choice, times
 
     def validation_error_model(self):
         m = _native.ValidationModel()

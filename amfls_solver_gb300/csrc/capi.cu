@@ -483,6 +483,17 @@ int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream,
     });
 }
 
+int amfls_gpu_csr_operator_schedule(const amfls_gpu_operator* op, int* chains,
+                                    double* microseconds) {
+    return guarded([&] {
+        if (chains == nullptr || microseconds == nullptr)
+            throw std::invalid_argument("schedule buffers must not be null");
+        const auto* csr = dynamic_cast<const amfls_gpu::CsrOperator*>(&deref(op));
+        if (csr == nullptr) throw std::invalid_argument("operator is not a CSR operator");
+        csr->single_column_schedule(chains, microseconds);
+    });
+}
+
 int amfls_gpu_solve_amfls_batch(int count, const amfls_gpu_operator* const* ops,
                                 const double* const* d_b, const amfls_gpu_options* options,
                                 double* const* d_solutions, amfls_gpu_result* results,

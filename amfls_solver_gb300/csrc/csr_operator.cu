@@ -299,24 +299,28 @@ constexpr long long kChainMinNonzeros = 1LL << 21;
 // that the groups of a window stay together), for the kernel's snake-order
 // assignment of tasks to warps.
 void make_tiles(const std::vector<long long>& off, int count, int E, int C, bool chains,
-                TileStore& ts, cudaStream_t stream) {
+                TileStore& ts, cudaStream_t stream, int force = -1) {
     using namespace csr_tiles;
     std::vector<int4> tiles;
     std::vector<int> split;
     std::vector<int2> chain, long_rows;
     std::vector<int> cost;  // dependent memory round trips of the task
     auto length = [&](int r) { return off[r + 1] - off[r]; };
-    if (chains) {
-        const char* mode = std::getenv("AMFLS_GB300_CSR_CHAINS");
-        const bool off_mode = mode && std::string(mode) == "0";
-        const bool any_size = mode && std::string(mode) == "1";
-        chains = !off_mode && count > 0 && (any_size || off[count] >= kChainMinNonzeros);
-    }
-    if (chains) {
-        std::vector<long long> lens(count);
-        for (int r = 0; r < count; ++r) lens[r] = length(r);
-        std::nth_element(lens.begin(), lens.begin() + count / 2, lens.end());
-        chains = lens[count / 2] <= kChainShort;
+    if (force >= 0) {  // the autotuner's candidates
+        chains = force == 1 && count > 0;
+    } else {
+        if (chains) {
+            const char* mode = std::getenv("AMFLS_GB300_CSR_CHAINS");
+            const bool off_mode = mode && std::string(mode) == "0";
+            const bool any_size = mode && std::string(mode) == "1";
+            chains = !off_mode && count > 0 && (any_size || off[count] >= kChainMinNonzeros);
+        }
+        if (chains) {
+            std::vector<long long> lens(count);
+            for (int r = 0; r < count; ++r) lens[r] = length(r);
+            std::nth_element(lens.begin(), lens.begin() + count / 2, lens.end());
+            chains = lens[count / 2] <= kChainShort;
+        }
     }
     const long long longer_than = chains ? kChainMax : E;
     const long long task = (long long)kRowTaskTiles * E;
@@ -515,6 +519,13 @@ void launch_tiles(const int* off, const int* idx, const V* val, const TileStore&
 
 }  // namespace
 
+// Autotuning of the single-column tiling: sides with at least this many
+// nonzeros time both tilings (row blocks, chain groups) at construction and
+// keep the faster when it beats the size / row-length rule's choice by at
+// least kTuneMargin; closer calls keep the rule's (deterministic) choice.
+constexpr long long kTuneMinNonzeros = 1LL << 18;
+constexpr double kTuneMargin = 0.10;
+
 struct CsrOperator::Side {
     long long* off = nullptr;  // count+1
     int* off32 = nullptr;      // count+1, padded (bulk-copy source)
@@ -525,7 +536,37 @@ struct CsrOperator::Side {
     int count = 0;
     TileStore one;             // single-column products: chain groups or row blocks, long rows
     TileStore many;            // row blocks of kEC elements: 2..8 columns
+    double tuned_us[2] = {0.0, 0.0};  // measured product time: row blocks, chain groups
 };
+
+namespace {
+
+// Mean device time of `reps` single-column products of one side over the
+// table `ts` (after two untimed ones), CUDA events on `stream`.
+double time_tiles(const int* off32, const int* idx, const double* val, const TileStore& ts,
+                  const double* x, double* y, double* scratch, unsigned* counter,
+                  cudaStream_t stream) {
+    Epilogue ep;
+    ep.out = y;
+    cudaEvent_t e0, e1;
+    AMFLS_CUDA(cudaEventCreate(&e0));
+    AMFLS_CUDA(cudaEventCreate(&e1));
+    constexpr int reps = 5;
+    for (int i = 0; i < 2; ++i)
+        launch_tiles<1, true>(off32, idx, val, ts, x, nullptr, 0, 1, ep, scratch, counter, stream);
+    AMFLS_CUDA(cudaEventRecord(e0, stream));
+    for (int i = 0; i < reps; ++i)
+        launch_tiles<1, true>(off32, idx, val, ts, x, nullptr, 0, 1, ep, scratch, counter, stream);
+    AMFLS_CUDA(cudaEventRecord(e1, stream));
+    AMFLS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    AMFLS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return 1e3 * ms / reps;
+}
+
+}  // namespace
 
 CsrOperator::CsrOperator(int rows, int cols, const long long* d_offsets,
                          const long long* d_indices, const double* d_values, long long nnz,
@@ -752,6 +793,7 @@ void CsrOperator::build(const long long* d_off, const long long* d_idx, const do
         AMFLS_CUDA(cudaStreamSynchronize(stream));
         make_tiles(host_off, sd->count, csr_tiles::kE1, 1, true, sd->one, stream);
         make_tiles(host_off, sd->count, csr_tiles::kEC, 8, false, sd->many, stream);
+        tune_single_column(*sd, host_off, stream);
     }
 
     // certified norm model
@@ -857,6 +899,44 @@ __global__ void narrow_values_kernel(const double* in, long long n, V* out) {
 }
 
 }  // namespace
+
+// The autotuner: time the rule's table and the other tiling on this side
+// (products of a zero vector: the memory traffic and the instruction stream
+// do not depend on the values) and keep the faster one when it wins by at
+// least kTuneMargin.  AMFLS_GB300_CSR_CHAINS (either value) turns it off.
+void CsrOperator::tune_single_column(Side& sd, const std::vector<long long>& host_off,
+                                     cudaStream_t stream) {
+    if (std::getenv("AMFLS_GB300_CSR_CHAINS") || sd.count <= 0 ||
+        host_off[sd.count] < kTuneMinNonzeros)
+        return;
+    const long long in = &sd == a_.get() ? cols_ : rows_;
+    TileStore alt;
+    make_tiles(host_off, sd.count, csr_tiles::kE1, 1, true, alt, stream, sd.one.chains ? 0 : 1);
+    double *x = nullptr, *y = nullptr;
+    AMFLS_CUDA(cudaMallocAsync(&x, sizeof(double) * in, stream));
+    AMFLS_CUDA(cudaMallocAsync(&y, sizeof(double) * sd.count, stream));
+    AMFLS_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * in, stream));
+    const double t_rule = time_tiles(sd.off32, sd.idx, sd.val, sd.one, x, y, scratch_, counter_,
+                                     stream);
+    const double t_alt = time_tiles(sd.off32, sd.idx, sd.val, alt, x, y, scratch_, counter_,
+                                    stream);
+    AMFLS_CUDA(cudaFreeAsync(x, stream));
+    AMFLS_CUDA(cudaFreeAsync(y, stream));
+    AMFLS_CUDA(cudaStreamSynchronize(stream));
+    sd.tuned_us[sd.one.chains ? 1 : 0] = t_rule;
+    sd.tuned_us[alt.chains ? 1 : 0] = t_alt;
+    if (t_alt < (1.0 - kTuneMargin) * t_rule) std::swap(sd.one, alt);
+    alt.release();
+}
+
+void CsrOperator::single_column_schedule(int chains[2], double microseconds[4]) const {
+    const Side* sides[2] = {a_.get(), t_.get()};
+    for (int i = 0; i < 2; ++i) {
+        chains[i] = sides[i]->one.chains ? 1 : 0;
+        microseconds[2 * i] = sides[i]->tuned_us[0];
+        microseconds[2 * i + 1] = sides[i]->tuned_us[1];
+    }
+}
 
 bool CsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
                            cudaStream_t stream) const {

@@ -1,6 +1,8 @@
 // FP64 CSR operator on the device (see csr_operator.cu).
 #pragma once
 
+#include <vector>
+
 #include <memory>
 
 #include "device_operator.hpp"
@@ -40,6 +42,10 @@ public:
                                  double* x_lo, int* finite, cudaStream_t s) const override;
     bool product1(bool transpose, const double* x, const Epilogue& ep,
                   cudaStream_t s) const override;
+    // Tiling of the single-column products per side (A, then the stored
+    // transpose): 1 = chain groups, 0 = row blocks; the autotuner's timings
+    // (microseconds per product, row blocks then chain groups, 0 = not timed).
+    void single_column_schedule(int chains[2], double microseconds[4]) const;
 
 private:
     friend class ReducedCsrOperator;
@@ -47,6 +53,8 @@ private:
     void build(const long long* d_off, const long long* d_idx, const double* d_val,
                cudaStream_t stream);
     void build_bins(Side& s, const int* d_bins, cudaStream_t stream);
+    void tune_single_column(Side& s, const std::vector<long long>& host_off,
+                            cudaStream_t stream);
     void fill_ids(int* ids, long long n, cudaStream_t stream);
     void product(bool transpose, const double* x, int block_cols, double* y,
                  cudaStream_t stream) const;
@@ -94,6 +102,10 @@ public:
     ValidationModel validation_error_model() const override { return model_; }
     bool product1(bool transpose, const double* x, const Epilogue& ep,
                   cudaStream_t s) const override;
+    // Tiling of the single-column products per side (A, then the stored
+    // transpose): 1 = chain groups, 0 = row blocks; the autotuner's timings
+    // (microseconds per product, row blocks then chain groups, 0 = not timed).
+    void single_column_schedule(int chains[2], double microseconds[4]) const;
 
 private:
     void product(bool transpose, const double* x, int block_cols, double* y,

@@ -254,8 +254,9 @@ def spmm_measurement(dev, stream, peak):
     op = amfls.DeviceOperator(csr_device(prob, dev))
     lib = _native.load()
     m, n, nnz = prob.rows, prob.cols, prob.nnz
+    choice, tuned = op.tile_schedule()
     out = {"workload": "csr_2000000x500000", "rows": m, "cols": n, "nnz": nnz, "peak_gbs": peak,
-           "unit": "GB/s"}
+           "unit": "GB/s", "tiling": choice, "autotuner_us": tuned}
     for cols in (1, 8):
         x = torch.randn(cols * n, dtype=torch.float64, device=dev)
         y = torch.randn(cols * m, dtype=torch.float64, device=dev)

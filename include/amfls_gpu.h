@@ -307,6 +307,19 @@ int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b
  * the call; synchronous. */
 int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream, double* seconds);
 
+/* The tiling of a CSR operator's single-column products (no counterpart in
+ * the reference, whose products are scalar loops; sparse_csr_operator.cpp:
+ * 203-269).  A side (A, or the stored transpose) is cut into warp tasks
+ * either as chain groups or as row blocks; sides of at least 2^18 nonzeros
+ * time both tilings when the operator is created and keep the faster one
+ * when it wins by at least 10% over the size / row-length rule's choice.
+ * chains[0], chains[1]: 1 when A's / the transpose's products use chain
+ * groups; microseconds[0..3]: the timed products of A with row blocks and
+ * with chain groups, then the transpose's (0 where not timed).  An operator
+ * that is not a CSR operator is AMFLS_GPU_INVALID_ARGUMENT. */
+int amfls_gpu_csr_operator_schedule(const amfls_gpu_operator* op, int* chains,
+                                    double* microseconds);
+
 /* Batched AMFLS (no counterpart in the reference): `count` independent
  * problems, problem i = (ops[i], d_b[i], options[i]) with its solution in
  * d_solutions[i] (a distinct operator per problem: an operator's products

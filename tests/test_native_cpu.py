@@ -105,3 +105,8 @@ def test_callback_operator_needs_both_products(lib):
     assert rc == 1 and b"apply and apply_transpose" in lib.amfls_gpu_last_error()
     rc = lib.amfls_gpu_callback_operator_create(10, 5, None, None, ctypes.byref(handle))
     assert rc == 1 and handle.value is None
+
+
+def test_schedule_query_rejects_null_buffers(lib):
+    rc = lib.amfls_gpu_csr_operator_schedule(None, None, None)
+    assert rc == 1
