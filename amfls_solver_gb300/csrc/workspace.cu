@@ -648,6 +648,11 @@ sweep_vc_kernel(double* const* __restrict__ panels, int n, const double* __restr
 // Grid of the sweep kernels: every block resident at once (so the balanced
 // task ranges are balanced per SM), set up once per device.
 int sweep_grid() {
+    // AMFLS_GB300_SWEEP_BLOCKS (measurements): a fixed grid instead
+    if (const char* v = std::getenv("AMFLS_GB300_SWEEP_BLOCKS")) {
+        const int g = std::atoi(v);
+        if (g > 0) return g;
+    }
     static int cached[64] = {};
     int dev = 0;
     AMFLS_CUDA(cudaGetDevice(&dev));
