@@ -23,7 +23,7 @@ class Options(ctypes.Structure):
                 ("stream", ctypes.c_uint64), ("maximum_depth", ctypes.c_int),
                 ("maximum_auxiliary_width", ctypes.c_int), ("auxiliary_width", ctypes.c_int),
                 ("stop_early", ctypes.c_int), ("time_operators", ctypes.c_int),
-                ("use_graphs", ctypes.c_int)]
+                ("use_graphs", ctypes.c_int), ("reduced_basis", ctypes.c_int)]
 
 
 class BaselineOptions(ctypes.Structure):
@@ -39,7 +39,9 @@ class Result(ctypes.Structure):
                 ("stop_reason", ctypes.c_int), ("metrics", ctypes.c_double * METRICS),
                 ("counters", ctypes.c_longlong * COUNTERS),
                 ("timings", ctypes.c_double * TIMINGS), ("trace_rows", ctypes.c_int),
-                ("kernel_launches", ctypes.c_longlong)]
+                ("kernel_launches", ctypes.c_longlong),
+                ("reduced_basis_levels", ctypes.c_longlong),
+                ("reduced_basis_fallbacks", ctypes.c_longlong)]
 
 
 class ValidationModel(ctypes.Structure):
@@ -76,6 +78,7 @@ EXPORTED = [
     "amfls_gpu_callback_operator_create", "amfls_gpu_default_baseline_options",
     "amfls_gpu_solve_lsqr", "amfls_gpu_solve_lsmr", "amfls_gpu_solve_amfls_replay",
     "amfls_gpu_probe_reorthogonalization", "amfls_gpu_csr_operator_schedule",
+    "amfls_gpu_probe_reorthogonalization_reduced",
 ]
 
 POLICY_FEATURES = 11

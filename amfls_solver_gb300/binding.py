@@ -12,6 +12,7 @@ CUDA tensors.
 from __future__ import annotations
 
 import ctypes
+import dataclasses
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -118,6 +119,11 @@ class SolveResult:
     trace_int: torch.Tensor
     status: int
     stop_reason: int
+    # GB300 extras (not in the reference's result): width-one levels whose
+    # first reorthogonalisation pass ran on the FP32 copy of the basis, and
+    # how many of them redid it in FP64
+    reduced_basis_levels: int = 0
+    reduced_basis_fallbacks: int = 0
 
     @property
     def success(self) -> bool:
@@ -344,9 +350,15 @@ class DeviceOperator:
 
 # --------------------------------------------------------------- solves ----
 
-def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options):
+def _with_extras(result: SolveResult, res) -> SolveResult:
+    """The GB300 counters of a native result struct added to a decoded result."""
+    return dataclasses.replace(result, reduced_basis_levels=int(res.reduced_basis_levels),
+                               reduced_basis_fallbacks=int(res.reduced_basis_fallbacks))
+
+
+def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options, native=None):
     """options: _native.Options (amfls, fixed_rbgk) or _native.BaselineOptions
-    (lsqr, lsmr)."""
+    (lsqr, lsmr); `native` (a list) receives the native result struct."""
     lib = _native.load()
     if b.device != op.device:
         raise ValueError("matrix and b must be on the same CUDA device")
@@ -361,6 +373,8 @@ def _solve_raw(algorithm: str, op: DeviceOperator, b: torch.Tensor, options):
                          ctypes.byref(res), tf.ctypes.data, ti.ctypes.data, TRACE_CAPACITY,
                          _stream_handle(b.device)))
     rows = min(res.trace_rows, TRACE_CAPACITY)
+    if native is not None:
+        native.append(res)
     return (x,
             torch.tensor(list(res.metrics), dtype=torch.float64),
             torch.tensor(list(res.counters), dtype=torch.int64),
@@ -378,10 +392,14 @@ def solve_amfls(op: DeviceOperator, b: torch.Tensor, *, regularization: float = 
                 tolerance: float = 1e-8, failure_probability: float = 1e-6,
                 maximum_epochs: int = 0, maximum_depth: int = 0,
                 maximum_auxiliary_width: int = 0, maximum_basis_size: int = 0, seed: int = 0,
-                stream: int = 0) -> SolveResult:
+                stream: int = 0, reduced_basis: bool = False) -> SolveResult:
     """AMFLS on an existing DeviceOperator (CSR, dense, reduced or callback),
     the reference's C++ entry amfls::solve_amfls(op, b, options)
-    (include/amfls/amfls.hpp:22-25)."""
+    (include/amfls/amfls.hpp:22-25).  reduced_basis (not a reference option)
+    runs the first reorthogonalisation pass of width-one levels on an FP32
+    copy of the right basis, the sweeps of the mixed form's restart cycles;
+    a single solve of an ill-conditioned problem to FP64 accuracy can stall
+    with it (the certificate reports that)."""
     if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
         raise ValueError("b must be a float64 CUDA vector of length rows on the operator's device")
     o = _native.default_options()
@@ -394,7 +412,9 @@ def solve_amfls(op: DeviceOperator, b: torch.Tensor, *, regularization: float = 
     o.maximum_basis_size = int(maximum_basis_size)
     o.seed = _uint64(seed)
     o.stream = _uint64(stream)
-    return _decode(_solve_raw("amfls", op, b, o))
+    o.reduced_basis = 1 if reduced_basis else 0
+    native = []
+    return _with_extras(_decode(_solve_raw("amfls", op, b, o, native)), native[0])
 
 
 def solve_amfls_replay(op: DeviceOperator, b: torch.Tensor, replay, *,
@@ -505,16 +525,26 @@ def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
                     failure_probability: float = 1e-6, maximum_epochs: int = 0,
                     maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
                     maximum_basis_size: int = 0, seed: int = 0, stream: int = 0,
-                    reduced: "DeviceOperator | None" = None) -> SolveResult:
-    """Mixed-precision AMFLS: FP32 (or BF16-stored) inner solves refined in
-    FP64; the certified FP64 validation on the original matrix decides
-    termination.  `matrix` is a CUDA tensor or a DeviceOperator; `reduced`
-    reuses an existing reduced operator.  Work limits apply to each inner
-    solve.  No counterpart in the reference."""
+                    reduced: "DeviceOperator | None" = None,
+                    reduced_basis: bool = False) -> SolveResult:
+    """Mixed-precision AMFLS: inner solves refined in FP64; the certified
+    FP64 validation on the original matrix decides termination.  `values`
+    is the inner products' precision ("fp32", "bf16", or "fp64" for inner
+    solves on the FP64 operator itself); `reduced_basis` runs the inner
+    solves' first reorthogonalisation pass on an FP32 copy of the basis.
+    With maximum_depth set and a tiny inner_tolerance every inner solve is
+    one restart cycle of maximum_depth levels.  `matrix` is a CUDA tensor or
+    a DeviceOperator; `reduced` reuses an existing reduced operator.  Work
+    limits apply to each inner solve.  No counterpart in the reference."""
     op = matrix if isinstance(matrix, DeviceOperator) else DeviceOperator(matrix)
     if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
         raise ValueError("b must be a float64 CUDA vector of length rows on the matrix's device")
-    low = reduced if reduced is not None else op.reduced(values)
+    if reduced is not None:
+        low = reduced
+    elif values == "fp64":
+        low = op
+    else:
+        low = op.reduced(values)
     o = _native.default_options()
     o.regularization = float(regularization)
     o.tolerance = float(tolerance)
@@ -525,6 +555,7 @@ def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
     o.maximum_basis_size = int(maximum_basis_size)
     o.seed = _uint64(seed)
     o.stream = _uint64(stream)
+    o.reduced_basis = 1 if reduced_basis else 0
     b = b.contiguous()
     x = torch.empty(op.cols, dtype=torch.float64, device=b.device)
     res = _native.Result()
@@ -536,11 +567,12 @@ def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
             int(maximum_refinements), x.data_ptr(), ctypes.byref(res), tf.ctypes.data,
             ti.ctypes.data, TRACE_CAPACITY, _stream_handle(b.device)))
     rows = min(res.trace_rows, TRACE_CAPACITY)
-    return _decode((x, torch.tensor(list(res.metrics), dtype=torch.float64),
-                    torch.tensor(list(res.counters), dtype=torch.int64),
-                    torch.tensor(list(res.timings), dtype=torch.float64),
-                    torch.from_numpy(tf[:rows].copy()), torch.from_numpy(ti[:rows].copy()),
-                    int(res.status), int(res.stop_reason)))
+    return _with_extras(_decode((x, torch.tensor(list(res.metrics), dtype=torch.float64),
+                                 torch.tensor(list(res.counters), dtype=torch.int64),
+                                 torch.tensor(list(res.timings), dtype=torch.float64),
+                                 torch.from_numpy(tf[:rows].copy()),
+                                 torch.from_numpy(ti[:rows].copy()),
+                                 int(res.status), int(res.stop_reason))), res)
 
 
 def _run_amfls_impl(matrix, b, regularization, tolerance, failure_probability,

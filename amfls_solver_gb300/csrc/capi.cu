@@ -79,6 +79,7 @@ amfls_gpu::SolveOptions to_options(const amfls_gpu_options* o) {
     s.stop_early = o->stop_early != 0;
     s.time_operators = o->time_operators != 0;
     s.use_graphs = o->use_graphs != 0;
+    s.reduced_basis = o->reduced_basis != 0;
     return s;
 }
 
@@ -98,6 +99,8 @@ void export_result(const amfls_gpu::SolveResult& r, amfls_gpu_result* out, doubl
     amfls_gpu::pack_timings(r, out->timings);
     out->trace_rows = static_cast<int>(r.trace.size());
     out->kernel_launches = r.statistics.kernel_launches;
+    out->reduced_basis_levels = r.statistics.reduced_levels;
+    out->reduced_basis_fallbacks = r.statistics.reduced_fallbacks;
     const int rows = std::min<int>(cap, static_cast<int>(r.trace.size()));
     for (int i = 0; i < rows; ++i) {
         if (tf) std::memcpy(tf + 29 * i, r.trace[i].f, sizeof(double) * 29);
@@ -480,6 +483,15 @@ int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream,
     return guarded([&] {
         if (seconds == nullptr) throw std::invalid_argument("seconds must not be null");
         amfls_gpu::probe_reorthogonalization(n, k, reps, as_stream(stream), seconds);
+    });
+}
+
+int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, void* stream,
+                                                double* seconds, double* max_rel_error) {
+    return guarded([&] {
+        if (seconds == nullptr) throw std::invalid_argument("seconds must not be null");
+        amfls_gpu::probe_reorthogonalization_reduced(n, k, reps, as_stream(stream), seconds,
+                                                     max_rel_error);
     });
 }
 

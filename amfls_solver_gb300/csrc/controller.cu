@@ -483,7 +483,7 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
     const long long launches0 = launch_count();
     Statistics stats;
     Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators,
-                 o.use_graphs && op.graph_safe());
+                 o.use_graphs && op.graph_safe(), o.reduced_basis);
     Evaluator ev(ws, op, d_b, reg, stats, stream);
     long long seen[4] = {0, 0, 0, 0};
     auto absorb = [&] {
@@ -557,12 +557,14 @@ SolveResult solve_amfls(const DeviceOperator& op, const double* d_b, const Solve
         stream_wait(stream);
         stats.total_seconds = seconds_since(t_start);
         stats.kernel_launches = launch_count() - launches0;
+        stats.reduced_levels = ws.state().reduced_levels;
+        stats.reduced_fallbacks = ws.state().reduced_fallbacks;
         out.statistics = stats;
         return out;
     };
     auto finish_self = [&](const Candidate& c) { return finish(c, c.v.status, c.v.stop_reason); };
     auto finish_at_limit = [&](int status, int reason) {
-        return finish(reg > 0.0 ? result : best, status, reason);
+        return finish(reg > 0.0 || o.latest_at_limit ? result : best, status, reason);
     };
 
     ws.initialize(nullptr, 0);
@@ -819,7 +821,7 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
     const long long launches0 = launch_count();
     Statistics stats;
     Workspace ws(op, d_b, reg, o.maximum_basis_size, stream, o.time_operators,
-                 o.use_graphs && op.graph_safe());
+                 o.use_graphs && op.graph_safe(), o.reduced_basis);
     Evaluator ev(ws, op, d_b, reg, stats, stream);
     long long seen[4] = {0, 0, 0, 0};
     auto absorb = [&] {
@@ -958,6 +960,8 @@ SolveResult solve_fixed_rbgk(const DeviceOperator& op, const double* d_b, const 
     stream_wait(stream);
     stats.total_seconds = seconds_since(t_start);
     stats.kernel_launches = launch_count() - launches0;
+    stats.reduced_levels = ws.state().reduced_levels;
+    stats.reduced_fallbacks = ws.state().reduced_fallbacks;
     out.statistics = stats;
     return out;
 }

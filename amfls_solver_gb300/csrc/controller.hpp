@@ -26,6 +26,19 @@ struct SolveOptions {
     bool stop_early = true;   // fixed RBGK only
     bool time_operators = true;
     bool use_graphs = true;
+    // At a work or basis limit return the latest checkpoint's candidate even
+    // for lambda = 0 (the reference returns the one with the smallest
+    // backward error there, amfls.cpp:156-163).  Not part of the reference's
+    // options: the mixed form's restarted inner solves use it, because the
+    // latest least-squares iterate has the smallest error in the normal
+    // equations' energy norm while the backward error need not be monotone.
+    bool latest_at_limit = false;
+    // Width-one levels keep an FP32 copy of the right basis and run their
+    // first reorthogonalisation pass on it, redoing it in FP64 when the
+    // coefficients are not small (see the reduced-basis sweeps in
+    // workspace.cu).  Not part of the reference's options: the
+    // mixed-precision form's reduced sweeps.
+    bool reduced_basis = false;
 };
 
 // RunStatistics (include/amfls/least_squares_result.hpp:57-109).
@@ -51,6 +64,8 @@ struct Statistics {
     // GB300 extras (not in the reference's tensors)
     long long projected_rank_flags = 0;
     long long kernel_launches = 0;  // kernels this solve ran on the GPU
+    long long reduced_levels = 0;     // levels projected on the FP32 copy of V
+    long long reduced_fallbacks = 0;  // of those, levels redone in FP64
 };
 
 struct TraceRow {

@@ -11,7 +11,13 @@
 //   d_k = argmin ||M~ d - s_k||   (AMFLS, lambda 0, on the reduced M~)
 //   x_{k+1} = x_k - d_k
 // until the FP64 certificate of x meets the tolerance, the certificate stops
-// shrinking by a factor of two after the first step, or the budget is spent.
+// shrinking (by a factor of two after a converged inner solve; at all after
+// an inner solve cut by maximum_depth), or the budget is spent.  With
+// maximum_depth set and a tiny inner tolerance each inner solve is one
+// restart cycle of L = maximum_depth levels (restarted CG on the normal
+// equations, whose latest iterate minimises the energy-norm error over its
+// Krylov space): the basis, and so the cost of its sweeps, stays bounded by
+// L instead of growing with the whole solve.
 // Each step contracts the error by about cond(M) u_low + the inner
 // tolerance.  The inner AMFLS stops on a backward error relative to the
 // correction problem, whose residual tends to s* = M x* - c, so when s* is
@@ -77,6 +83,8 @@ void accumulate(Statistics& into, const Statistics& s) {
     into.validation_seconds += s.validation_seconds;
     into.base_validation_seconds += s.base_validation_seconds;
     into.projected_rank_flags += s.projected_rank_flags;
+    into.reduced_levels += s.reduced_levels;
+    into.reduced_fallbacks += s.reduced_fallbacks;
 }
 
 void count_validation(Statistics& s, const ValidationOutput& v) {
@@ -147,6 +155,9 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
     SolveOptions io = o;
     io.regularization = 0.0;
     io.tolerance = inner_tolerance;
+    // an inner solve cut by maximum_depth is a restart cycle: its latest
+    // iterate is the best correction in the energy norm
+    io.latest_at_limit = true;
     double best = __builtin_huge_val();
     for (int k = 0; k < maximum_refinements; ++k) {
         io.stream = o.stream + (std::uint64_t)k;
@@ -189,7 +200,11 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
             steps->push_back(RefinementStep{xr.status, xr.stop_reason, xr.depth, xr.basis_rank,
                                             cert});
         if (v.status == 0) break;
-        if (k > 0 && !(cert < 0.5 * best)) break;  // no longer contracting
+        // no longer contracting: an inner solve that converged (no depth
+        // limit) must halve the certificate; a restart cycle (stopped by
+        // maximum_depth) must still reduce it
+        const bool cycle = xr.stop_reason == 3;
+        if (k > 0 && !(cert < (cycle ? 0.99 : 0.5) * best)) break;
         best = std::min(best, cert);
         // s_{k+1} = M x_{k+1} - c in FP64 (A x - b, then sqrt(lambda) x)
         Epilogue ep;

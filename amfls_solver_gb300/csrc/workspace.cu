@@ -250,6 +250,7 @@ __global__ void level_begin_kernel(DevState* st) {
     st->right_rank = 0;
     st->left_rank = 0;
     st->coeff_nonfinite = 0;
+    st->sweep_fp64 = 0;
     st->level_ok = 0;
     st->search_at_calls += 1;
     st->search_at_columns += st->left_width + st->pending;
@@ -272,8 +273,8 @@ __global__ void right_scales_kernel(DevState* st, const RedResult* red, int m, i
 __global__ void __launch_bounds__(kThreads)
 vt_r_kernel(double* const* __restrict__ panels, int n, int chunk_rows,
             const double* __restrict__ r, double* __restrict__ c, double* partials,
-            unsigned* panel_tickets, DevState* st, int pass) {
-    if (!st->go || (pass == 2 && !st->second_pass)) return;
+            unsigned* panel_tickets, DevState* st, int pass, int only_fp64 = 0) {
+    if (!st->go || (pass == 2 && !st->second_pass) || (only_fp64 && !st->sweep_fp64)) return;
     const int k = st->k;  // k == 0: no projection (decided in right_scales_kernel)
     const int p = blockIdx.x, chunk = blockIdx.y, nchunks = gridDim.y;
     if (p * 32 >= k) return;  // panel beyond the current basis
@@ -345,11 +346,15 @@ vt_r_kernel(double* const* __restrict__ panels, int n, int chunk_rows,
 
 // out = r - V c (subtract) or out = V c; 32 rows per block, warps split the
 // panels.  Sum of squares of out reduced by the last block, then `hook`.
+// guarded: 0 always runs, 1 runs when the level (and pass) runs, 2 as 1 but
+// only when a reduced-basis level redoes its projection in FP64.
 __global__ void __launch_bounds__(kThreads)
 v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* __restrict__ c,
            const double* r_in, double* out, int subtract, double* partials, unsigned* ticket,
            DevState* st, int hook, int m_rows, int guarded, int pass) {
-    if (guarded && (!st->go || (pass == 2 && !st->second_pass) || st->k == 0)) return;
+    if (guarded && (!st->go || (pass == 2 && !st->second_pass) || st->k == 0 ||
+                    (guarded == 2 && !st->sweep_fp64)))
+        return;
     const int k = k_arg >= 0 ? k_arg : st->k;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int q = lane & 3, rsub = lane >> 2;
@@ -428,6 +433,288 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
             }
         }
     }
+}
+
+// ----------------------------------------------------------------------------
+// Reduced-basis sweeps: width-one levels that keep an FP32 copy V~ of V run
+// their first projection pass on it,
+//   c  = V~^T r~          r~ = fl32(r); FP32 products, FP32 sums over runs of
+//                         16 rows per lane, FP64 above that
+//   r <- r - fl64(V~ c~)  c~ = fl32(c); FP32 products and sums, the
+//                         subtraction in FP64
+// At width one the recurrence has already removed the previous column in
+// FP64 (the fused A^T u - beta v product), so the pass-one coefficients only
+// measure the loss of orthogonality of r against V.  Rounding V and r to
+// FP32 perturbs each coefficient by about u32 ||r|| / sqrt(n_eff) (n_eff the
+// rows the vectors spread over), which is the level of orthogonality V keeps
+// instead of FP64's; the FP32 sum V~ c~ perturbs r itself by about
+// u32 ||V c|| (at most 6e-11 ||r|| while ||c|| <= kReducedCoeffBound ||r||).
+// A level whose coefficients exceed that bound (or are not finite) redoes
+// the pass with the FP64 kernels, and the DGKS second pass is always FP64,
+// so FP64 stays on the recurrence, the correction of large components, the
+// norms and every rank decision.  The sweeps then read 4 bytes per basis
+// element on the FP32 pipe (HBM-bound) instead of 8 bytes on the FP64 pipe
+// (two FMA lanes per SM clock on this GPU).
+// The orthogonality this keeps suits the restart cycles of the mixed form,
+// whose corrections need a few digits each: with one-sided
+// reorthogonalisation the left basis U inherits V's orthogonality level
+// amplified by about cond(A), so a single solve of an ill-conditioned
+// problem to FP64 accuracy stalls on it (the certificate then reports the
+// failure; it never certifies a wrong x).
+constexpr double kReducedCoeffBound = 1e-3;
+
+// r~ = fl32(r) for the reduced pass (only when the level projects).
+__global__ void round_residual_kernel(const double* __restrict__ r, float* __restrict__ r32, int n,
+                                      const DevState* st) {
+    if (!st->go || st->k == 0) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        r32[i] = __double2float_rn(r[i]);
+}
+
+// Row chunks per panel of vt_r32_kernel on `grid` blocks: about four
+// (panel, chunk) tasks per block, at least 256 rows per chunk.
+__host__ __device__ inline int reduced_chunks(long long n, int panels, int grid) {
+    const long long want = (4LL * grid + panels - 1) / panels;
+    const long long most = (n + 255) / 256;
+    return (int)(want < 1 ? 1 : (want < most ? want : (most < 1 ? 1 : most)));
+}
+
+// Partial-sum doubles vt_r32_kernel needs for up to `panels` panels.
+inline long long reduced_part_doubles(int grid, long long panels) {
+    return (4LL * grid + panels + 1) * 32;
+}
+
+// c = V~^T r~ over the (panel, row chunk) tasks of the current basis, taken
+// by the blocks in a fixed round robin.  The chunks of a panel are added in
+// chunk order by the block that finishes the panel last; the block that
+// finishes the last panel adds the panels' sums of c^2 in panel order and
+// decides whether the level redoes the pass in FP64.  Deterministic for a
+// fixed grid.
+__global__ void __launch_bounds__(kThreads)
+vt_r32_kernel(const float* const* __restrict__ panels, int n, const float* __restrict__ r,
+              double* __restrict__ c, float* __restrict__ c32, double* part, double* panel_sq,
+              unsigned* panel_tickets, unsigned* all_ticket, DevState* st) {
+    if (!st->go) return;
+    const int k = st->k;
+    if (k == 0) return;
+    const int P = (k + 31) / 32;
+    const int chunks = reduced_chunks(n, P, gridDim.x);
+    const long long chunk_rows = ((long long)n + chunks - 1) / chunks;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int q = lane & 3, rsub = lane >> 2;
+    __shared__ double sm[8][32];
+    __shared__ int last;
+    for (int t = blockIdx.x; t < P * chunks; t += gridDim.x) {
+        const int p = t / chunks, chunk = t - p * chunks;
+        const float* __restrict__ vp = panels[p];
+        const long long row0 = (long long)chunk * chunk_rows;
+        const long long row1 = min((long long)n, row0 + chunk_rows);
+        double acc[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+        // a warp covers 32 rows per step (rows base + 8j + rsub), a block 256
+        long long base = row0 + warp * 32;
+        while (base < row1) {
+            float s8[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s8[i] = 0.f;
+            for (int step = 0; step < 4 && base < row1; ++step, base += 256) {
+                float4 a[4][2];
+                float rv[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const long long row = base + j * 8 + rsub;
+                    if (row < row1) {
+                        const float4* src = reinterpret_cast<const float4*>(vp + row * 32 + q * 8);
+                        a[j][0] = __ldcs(src);
+                        a[j][1] = __ldcs(src + 1);
+                        rv[j] = __ldg(r + row);
+                    } else {
+                        a[j][0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        a[j][1] = a[j][0];
+                        rv[j] = 0.f;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    s8[0] = fmaf(a[j][0].x, rv[j], s8[0]);
+                    s8[1] = fmaf(a[j][0].y, rv[j], s8[1]);
+                    s8[2] = fmaf(a[j][0].z, rv[j], s8[2]);
+                    s8[3] = fmaf(a[j][0].w, rv[j], s8[3]);
+                    s8[4] = fmaf(a[j][1].x, rv[j], s8[4]);
+                    s8[5] = fmaf(a[j][1].y, rv[j], s8[5]);
+                    s8[6] = fmaf(a[j][1].z, rv[j], s8[6]);
+                    s8[7] = fmaf(a[j][1].w, rv[j], s8[7]);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] += (double)s8[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 4);
+            acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 8);
+            acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 16);
+        }
+        if (lane < 4) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) sm[warp][lane * 8 + i] = acc[i];
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double v = 0.0;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) v += sm[w][threadIdx.x];
+            part[((long long)p * chunks + chunk) * 32 + threadIdx.x] = v;
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned tk = atomicAdd(&panel_tickets[p], 1u);
+            last = tk == (unsigned)chunks - 1;
+            if (last) panel_tickets[p] = 0u;
+        }
+        __syncthreads();
+        if (last && threadIdx.x < 32) {  // warp 0 closes the panel
+            __threadfence();
+            double v = 0.0;
+            for (int ch = 0; ch < chunks; ++ch)
+                v += __ldcg(&part[((long long)p * chunks + ch) * 32 + threadIdx.x]);
+            const int col = p * 32 + threadIdx.x;
+            double sq = 0.0;
+            if (col < k) {
+                c[col] = v;
+                c32[col] = __double2float_rn(v);
+                sq = v * v;
+            }
+            sq = warp_sum(sq);
+            if (threadIdx.x == 0) {
+                panel_sq[p] = sq;
+                __threadfence();
+                const unsigned a = atomicAdd(all_ticket, 1u);
+                if (a == (unsigned)P - 1) {
+                    *all_ticket = 0u;
+                    __threadfence();
+                    double tot = 0.0;
+                    for (int pp = 0; pp < P; ++pp) tot += __ldcg(&panel_sq[pp]);
+                    const double before = st->norm_before;
+                    const double bound = kReducedCoeffBound * before;
+                    const bool redo = !(isfinite(tot) && isfinite(before)) || tot > bound * bound;
+                    st->sweep_fp64 = redo ? 1 : 0;
+                    st->reduced_levels += 1;
+                    if (redo) st->reduced_fallbacks += 1;
+                }
+            }
+        }
+        __syncthreads();  // sm and `last` are reused by the next task
+    }
+}
+
+// r <- r - fl64(V~ c~) with ||r||^2 and the DGKS decision of the first pass
+// (as v_c_kernel's kHookRightPass1); 32 rows per block, warps split the
+// panels.  Skipped when the level redoes the pass in FP64.
+__global__ void __launch_bounds__(kThreads)
+v_c32_kernel(const float* const* __restrict__ panels, int n, const float* __restrict__ c,
+             double* r, double* partials, unsigned* ticket, DevState* st, int m_rows) {
+    if (!st->go || st->k == 0 || st->sweep_fp64) return;
+    const int k = st->k;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int q = lane & 3, rsub = lane >> 2;
+    const long long row0 = (long long)blockIdx.x * 32;
+    const int P = (k + 31) / 32;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+    for (int p = warp; p < P; p += 8) {
+        const float* __restrict__ vp = panels[p];
+        float cv[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int col = p * 32 + q * 8 + i;
+            cv[i] = col < k ? c[col] : 0.f;
+        }
+        float4 a[4][2];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const long long row = row0 + s * 8 + rsub;
+            if (row < n) {
+                const float4* src = reinterpret_cast<const float4*>(vp + row * 32 + q * 8);
+                a[s][0] = __ldcs(src);
+                a[s][1] = __ldcs(src + 1);
+            } else {
+                a[s][0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                a[s][1] = a[s][0];
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            float t = acc[s];
+            t = fmaf(a[s][0].x, cv[0], t);
+            t = fmaf(a[s][0].y, cv[1], t);
+            t = fmaf(a[s][0].z, cv[2], t);
+            t = fmaf(a[s][0].w, cv[3], t);
+            t = fmaf(a[s][1].x, cv[4], t);
+            t = fmaf(a[s][1].y, cv[5], t);
+            t = fmaf(a[s][1].z, cv[6], t);
+            t = fmaf(a[s][1].w, cv[7], t);
+            acc[s] = t;
+        }
+    }
+    double accd[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        accd[s] = (double)acc[s];
+        accd[s] += __shfl_xor_sync(0xffffffffu, accd[s], 1);
+        accd[s] += __shfl_xor_sync(0xffffffffu, accd[s], 2);
+    }
+    __shared__ double sm[8][32];
+    __shared__ double red[32];
+    if (q == 0) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) sm[warp][s * 8 + rsub] = accd[s];
+    }
+    __syncthreads();
+    double sq = 0.0;
+    if (threadIdx.x < 32) {
+        const long long row = row0 + threadIdx.x;
+        double y = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) y += sm[w][threadIdx.x];
+        if (row < n) {
+            const double o = r[row] - y;
+            r[row] = o;
+            sq = o * o;
+        }
+    }
+    const double bs = block_sum(sq, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+    if (arrive_last(ticket, gridDim.x)) {
+        double a = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) a += partials[b];
+        a = block_sum(a, red);
+        if (threadIdx.x == 0) {
+            st->norm_after = sqrt(a);
+            const double before = st->norm_before, after = st->norm_after;
+            const bool again = isfinite(before) && isfinite(after) &&
+                               after < 0.70710678118654757 * before;
+            st->second_pass = again ? 1 : 0;
+            if (!again) decide_right(st, m_rows, n);
+        }
+    }
+}
+
+// Blocks of vt_r32_kernel: as many as are resident at once.
+int reduced_sweep_grid() {
+    static int cached[64] = {};
+    int dev = 0;
+    AMFLS_CUDA(cudaGetDevice(&dev));
+    const int slot = dev >= 0 && dev < 64 ? dev : 0;
+    if (cached[slot] == 0) {
+        int a = 0;
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, vt_r32_kernel, kThreads, 0));
+        cached[slot] = std::max(1, a) * sm_count();
+    }
+    return cached[slot];
 }
 
 // ----------------------------------------------------------------------------
@@ -676,18 +963,23 @@ long long sweep_part_doubles(int n, long long panels, int grid) {
     return (kSweepTargetTasksPerWarp * W + std::max(panels, tiles) + 1) * 32;
 }
 
+// v = r / ||r|| into V's new column (and the FP32 copy's, when kept) and a
+// contiguous copy.
 __global__ void normalize_right_kernel(const double* r, int n, double* const* panels,
-                                       double* vnew, DevState* st) {
+                                       double* vnew, DevState* st,
+                                       float* const* panels32 = nullptr) {
     if (!st->go || !st->right_rank) return;
     const double inv = st->inv_right;
     const int k = st->k;
     double* vcol = panels[k >> 5] + (k & 31);
+    float* vcol32 = panels32 ? panels32[k >> 5] + (k & 31) : nullptr;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_mark = global_ns();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const double v = r[i] * inv;
         vcol[i * 32] = v;
         vnew[i] = v;
+        if (vcol32) vcol32[i * 32] = __double2float_rn(v);
     }
 }
 
@@ -858,41 +1150,49 @@ __global__ void projected_solve_kernel(const double* alpha, const double* beta, 
 
 // ------------------------------------------------------------ panels ----
 
-PanelStore::PanelStore(int n, int max_panels, cudaStream_t stream)
+template <typename T>
+PanelStoreT<T>::PanelStoreT(int n, int max_panels, cudaStream_t stream)
     : n_(n), stream_(stream), table_cap_(std::max(1, max_panels)) {
     // fixed-capacity device table: its address never changes, so captured
     // kernels may keep it
-    stream_alloc(&table_, sizeof(double*) * table_cap_, stream_);
+    stream_alloc(&table_, sizeof(T*) * table_cap_, stream_);
     host_.reserve(table_cap_);
 }
 
-PanelStore::~PanelStore() {
-    for (double* p : host_) stream_free(p, stream_);
+template <typename T>
+PanelStoreT<T>::~PanelStoreT() {
+    for (T* p : host_) stream_free(p, stream_);
     stream_free(table_, stream_);
 }
 
-void PanelStore::ensure_columns(int cols) {
+template <typename T>
+void PanelStoreT<T>::ensure_columns(int cols) {
     const int need = (cols + 31) / 32;
     if (need <= panels()) return;
     if (need > table_cap_) throw std::length_error("basis exceeds the panel table capacity");
     const int first = panels();
     while (panels() < need) {
-        double* p = nullptr;
-        stream_alloc(&p, sizeof(double) * 32 * static_cast<size_t>(n_), stream_);
-        AMFLS_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * 32 * static_cast<size_t>(n_), stream_));
+        T* p = nullptr;
+        // zeroed: the sweeps read whole panels and mask columns beyond k by
+        // their coefficients, which needs finite (zero) entries there
+        stream_alloc(&p, sizeof(T) * 32 * static_cast<size_t>(n_), stream_);
+        AMFLS_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * 32 * static_cast<size_t>(n_), stream_));
         host_.push_back(p);
     }
     // host_ never reallocates (reserved to table_cap_), so the async copy
     // reads stable memory
     AMFLS_CUDA(cudaMemcpyAsync(table_ + first, host_.data() + first,
-                               sizeof(double*) * (need - first), cudaMemcpyHostToDevice, stream_));
+                               sizeof(T*) * (need - first), cudaMemcpyHostToDevice, stream_));
 }
+
+template class PanelStoreT<double>;
+template class PanelStoreT<float>;
 
 // --------------------------------------------------------- workspace ----
 
 Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regularization,
                      int maximum_basis_size, cudaStream_t stream, bool time_operators,
-                     bool use_graphs)
+                     bool use_graphs, bool reduced_basis)
     : op_(op), stream_(stream), m_(op.rows()), n_(op.cols()), reg_(regularization),
       time_ops_(time_operators), use_graphs_(use_graphs), b_(d_b) {
     if (m_ <= 0 || n_ <= 0) throw std::invalid_argument("block Golub-Kahan operator dimensions must be positive");
@@ -931,6 +1231,18 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     stream_alloc(&U_, sizeof(double) * m_ * ucap_, stream_);
     V_ = std::make_unique<PanelStore>(n_, static_cast<int>(max_panels), stream_);
     V_->ensure_columns(1);  // panel 0 exists (zeroed) before any level runs
+    reduced_basis_ = reduced_basis;
+    if (reduced_basis_) {
+        V32_ = std::make_unique<PanelStore32>(n_, static_cast<int>(max_panels), stream_);
+        V32_->ensure_columns(1);
+        red_grid_ = reduced_sweep_grid();
+        stream_alloc(&r32_, sizeof(float) * n_, stream_);
+        stream_alloc(&panel_sq_, sizeof(double) * max_panels, stream_);
+        stream_alloc(&red_part_, sizeof(double) * reduced_part_doubles(red_grid_, max_panels),
+                     stream_);
+        stream_alloc(&red_tickets_, sizeof(unsigned) * (max_panels + 1), stream_);
+        AMFLS_CUDA(cudaMemsetAsync(red_tickets_, 0, sizeof(unsigned) * (max_panels + 1), stream_));
+    }
     AMFLS_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
     std::memset(&host_, 0, sizeof(host_));
     host_.reliable = 1;
@@ -958,6 +1270,11 @@ Workspace::~Workspace() {
     stream_free(P_, stream_);
     stream_free(c1_, stream_);
     stream_free(c2_, stream_);
+    stream_free(c32_, stream_);
+    stream_free(r32_, stream_);
+    stream_free(panel_sq_, stream_);
+    stream_free(red_part_, stream_);
+    stream_free(red_tickets_, stream_);
     stream_free(alpha_, stream_);
     stream_free(beta_, stream_);
     stream_free(g_, stream_);
@@ -1007,6 +1324,12 @@ void Workspace::ensure_t_capacity(int cols) {
     grow(g_, old, cap);
     grow(c1_, old, cap);
     grow(c2_, old, cap);
+    if (reduced_basis_) {  // rewritten by every level before use: no copy
+        stream_free(c32_, stream_);
+        c32_ = nullptr;
+        stream_alloc(&c32_, sizeof(float) * cap, stream_);
+        AMFLS_CUDA(cudaMemsetAsync(c32_, 0, sizeof(float) * cap, stream_));
+    }
     // the QR arrays are laid out by capacity: rebuild them from scratch
     stream_free(qr_, stream_);
     qr_ = nullptr;
@@ -1091,10 +1414,34 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     const int max_chunks = (int)std::max<long long>(1, (n_ + 255) / 256);
     const int chunks = std::max(1, std::min(max_chunks, (gemv_target_blocks() + pcap - 1) / pcap));
     const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
-    for (int pass = 1; pass <= 2; ++pass) {
+    const bool reduced = reduced_basis_ && !block_mode_;
+    if (reduced) {
+        // first pass on the FP32 copy of V; the FP64 kernels after it run
+        // only when the coefficients were too large for it (sweep_fp64)
+        round_residual_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0,
+                                s>>>(R_, r32_, n_, dstate_);
+        AMFLS_LAUNCHED();
+        vt_r32_kernel<<<red_grid_, kThreads, 0, s>>>(V32_->device_table(), n_, r32_, c1_, c32_,
+                                                     red_part_, panel_sq_, red_tickets_,
+                                                     red_tickets_ + sweep_panels_, dstate_);
+        AMFLS_LAUNCHED();
+        vt_r_kernel<<<dim3(pcap, chunks), kThreads, 0, s>>>(V_->device_table(), n_, chunk_rows,
+                                                            R_, c1_, partials_, counter_ + 64,
+                                                            dstate_, 1, 1);
+        AMFLS_LAUNCHED();
+        v_c32_kernel<<<(int)tiles, kThreads, 0, s>>>(V32_->device_table(), n_, c32_, R_,
+                                                     partials_ + vc_partials_offset_, counter_ + 3,
+                                                     dstate_, m_);
+        AMFLS_LAUNCHED();
+        v_c_kernel<<<(int)tiles, kThreads, 0, s>>>(
+            V_->device_table(), n_, -1, c1_, R_, R_, 1, partials_ + vc_partials_offset_,
+            counter_ + 3, dstate_, kHookRightPass1, m_, 2, 1);
+        AMFLS_LAUNCHED();
+    }
+    for (int pass = reduced ? 2 : 1; pass <= 2; ++pass) {
         double* c = pass == 1 ? c1_ : c2_;
         const int hook = pass == 1 ? kHookRightPass1 : kHookRightPass2;
-        if (warp_sweeps_) {
+        if (warp_sweeps_ && !reduced) {
             sweep_vt_kernel<<<sweep_grid_, kThreads, 0, s>>>(V_->device_table(), n_, R_, c,
                                                              sweep_part_, panel_tickets, dstate_,
                                                              pass);
@@ -1115,7 +1462,7 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
         }
     }
     normalize_right_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0, s>>>(
-        R_, n_, V_->device_table(), vnew_, dstate_);
+        R_, n_, V_->device_table(), vnew_, dstate_, reduced ? V32_->device_table() : nullptr);
     AMFLS_LAUNCHED();
     // y = A v - ||r|| u, with ||A v||, ||y||, u.y
     Epilogue el;
@@ -1192,6 +1539,7 @@ void Workspace::advance_to(int target_depth) {
     // runs the whole interval without the host
     ensure_t_capacity(host_.k + levels + 2);
     V_->ensure_columns(host_.k + levels + 1);
+    if (V32_) V32_->ensure_columns(host_.k + levels + 1);
     const int pneed = (host_.k + levels + 31) / 32;
     int pcap = 4;
     while (pcap < pneed) pcap *= 2;
@@ -1279,7 +1627,123 @@ __global__ void probe_fill_kernel(double* const* panels, int n, int k, double* r
     }
 }
 
+__global__ void probe_round_kernel(double* const* panels, float* const* panels32, int n, int k,
+                                   const double* r, float* r32) {
+    const long long total = (long long)n * 32;
+    const int P = (k + 31) / 32;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total * P;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(i / total);
+        const long long e = i - (long long)p * total;
+        panels32[p][e] = __double2float_rn(panels[p][e]);
+        if (p == 0 && e % 32 == 0) r32[e / 32] = __double2float_rn(r[e / 32]);
+    }
+}
+
 }  // namespace
+
+void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, double seconds[2],
+                                       double* max_rel_error) {
+    if (n <= 0 || k <= 0 || reps <= 0) throw std::invalid_argument("probe sizes must be positive");
+    const int P = (k + 31) / 32;
+    PanelStore V(n, P, s);
+    PanelStore32 V32(n, P, s);
+    V.ensure_columns(k);
+    V32.ensure_columns(k);
+    const int grid = reduced_sweep_grid();
+    const long long tiles = (n + 31) / 32;
+    double *r = nullptr, *c = nullptr, *c64 = nullptr, *part = nullptr, *psq = nullptr,
+           *vcpart = nullptr;
+    float *r32 = nullptr, *c32 = nullptr;
+    unsigned* tickets = nullptr;
+    DevState* st = nullptr;
+    stream_alloc(&r, sizeof(double) * n, s);
+    stream_alloc(&r32, sizeof(float) * n, s);
+    stream_alloc(&c, sizeof(double) * 32 * P, s);
+    stream_alloc(&c64, sizeof(double) * 32 * P, s);
+    stream_alloc(&c32, sizeof(float) * 32 * P, s);
+    stream_alloc(&part, sizeof(double) * reduced_part_doubles(grid, P), s);
+    stream_alloc(&psq, sizeof(double) * P, s);
+    stream_alloc(&vcpart, sizeof(double) * (tiles + 1), s);
+    stream_alloc(&tickets, sizeof(unsigned) * (2 * P + 2), s);
+    stream_alloc(&st, sizeof(DevState), s);
+    AMFLS_CUDA(cudaMemsetAsync(tickets, 0, sizeof(unsigned) * (2 * P + 2), s));
+    DevState h;
+    std::memset(&h, 0, sizeof(h));
+    h.k = k;
+    h.go = 1;
+    h.reliable = 1;
+    h.basis_limit = k + 1;
+    h.right_scale = 1.0;
+    h.norm_before = 1e300;  // the pass never decides the level: state stays as set
+    AMFLS_CUDA(cudaMemcpyAsync(st, &h, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    probe_fill_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), n, k, r);
+    AMFLS_LAUNCHED();
+    probe_round_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), V32.device_table(), n, k, r,
+                                                  r32);
+    AMFLS_LAUNCHED();
+    // the FP64 projection of the same basis, for the error
+    {
+        const int chunks = std::max(1, std::min((int)std::max<long long>(1, (n + 255) / 256),
+                                                (gemv_target_blocks() + P - 1) / P));
+        const int chunk_rows = (int)(((long long)n + chunks - 1) / chunks);
+        vt_r_kernel<<<dim3(P, chunks), kThreads, 0, s>>>(V.device_table(), n, chunk_rows, r, c64,
+                                                         part, tickets, st, 1);
+        AMFLS_LAUNCHED();
+    }
+    auto vt = [&] {
+        vt_r32_kernel<<<grid, kThreads, 0, s>>>(V32.device_table(), n, r32, c, c32, part, psq,
+                                                tickets, tickets + 2 * P + 1, st);
+        AMFLS_LAUNCHED();
+    };
+    // r is restored by the caller's pattern only once; the subtraction of
+    // the tiny probe coefficients leaves it finite, which is all timing needs
+    auto vc = [&] {
+        v_c32_kernel<<<(int)tiles, kThreads, 0, s>>>(V32.device_table(), n, c32, r, vcpart,
+                                                     tickets + P, st, n);
+        AMFLS_LAUNCHED();
+    };
+    vt();
+    std::vector<double> hc(k), hc64(k), hr(n);
+    AMFLS_CUDA(cudaMemcpyAsync(hc.data(), c, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    AMFLS_CUDA(cudaMemcpyAsync(hc64.data(), c64, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    AMFLS_CUDA(cudaMemcpyAsync(hr.data(), r, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    stream_wait(s);
+    double rn = 0.0, worst = 0.0;
+    for (double v : hr) rn += v * v;
+    rn = std::sqrt(rn);
+    for (int j = 0; j < k; ++j) worst = std::max(worst, std::fabs(hc[j] - hc64[j]));
+    if (max_rel_error) *max_rel_error = rn > 0.0 ? worst / rn : worst;
+    cudaEvent_t e[3];
+    for (auto& ev : e) AMFLS_CUDA(cudaEventCreate(&ev));
+    for (int i = 0; i < 3; ++i) {  // warm-up
+        vt();
+        vc();
+    }
+    AMFLS_CUDA(cudaEventRecord(e[0], s));
+    for (int i = 0; i < reps; ++i) vt();
+    AMFLS_CUDA(cudaEventRecord(e[1], s));
+    for (int i = 0; i < reps; ++i) vc();
+    AMFLS_CUDA(cudaEventRecord(e[2], s));
+    AMFLS_CUDA(cudaEventSynchronize(e[2]));
+    float ms0 = 0.f, ms1 = 0.f;
+    AMFLS_CUDA(cudaEventElapsedTime(&ms0, e[0], e[1]));
+    AMFLS_CUDA(cudaEventElapsedTime(&ms1, e[1], e[2]));
+    for (auto& ev : e) cudaEventDestroy(ev);
+    seconds[0] = ms0 * 1e-3 / reps;
+    seconds[1] = ms1 * 1e-3 / reps;
+    stream_free(r, s);
+    stream_free(r32, s);
+    stream_free(c, s);
+    stream_free(c64, s);
+    stream_free(c32, s);
+    stream_free(part, s);
+    stream_free(psq, s);
+    stream_free(vcpart, s);
+    stream_free(tickets, s);
+    stream_free(st, s);
+    stream_wait(s);
+}
 
 void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double seconds[2]) {
     if (n <= 0 || k <= 0 || reps <= 0) throw std::invalid_argument("probe sizes must be positive");

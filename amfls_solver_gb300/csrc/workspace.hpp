@@ -29,30 +29,37 @@
 namespace amfls_gpu {
 
 
-class PanelStore {
+// Panels of 32 columns, each a row-major n x 32 tile, with a device table of
+// their addresses.  T = double holds V; T = float its reduced-basis shadow.
+template <typename T>
+class PanelStoreT {
 public:
-    PanelStore(int n, int max_panels, cudaStream_t stream);
-    ~PanelStore();
+    PanelStoreT(int n, int max_panels, cudaStream_t stream);
+    ~PanelStoreT();
     void ensure_columns(int cols);  // allocate (zeroed) panels to hold `cols` columns
-    double* column(int j) const { return host_[j / 32] + (j % 32); }  // stride 32
-    double* const* device_table() const { return table_; }
+    T* column(int j) const { return host_[j / 32] + (j % 32); }  // stride 32
+    T* const* device_table() const { return table_; }
     int panels() const { return static_cast<int>(host_.size()); }
     int n() const { return n_; }
-    size_t bytes() const { return host_.size() * static_cast<size_t>(n_) * 32 * sizeof(double); }
+    size_t bytes() const { return host_.size() * static_cast<size_t>(n_) * 32 * sizeof(T); }
 
 private:
     int n_;
     cudaStream_t stream_;
-    std::vector<double*> host_;
-    double** table_ = nullptr;
+    std::vector<T*> host_;
+    T** table_ = nullptr;
     int table_cap_ = 0;
 };
+using PanelStore = PanelStoreT<double>;
+using PanelStore32 = PanelStoreT<float>;
 
 class Workspace {
 public:
+    // reduced_basis: width-one levels keep an FP32 copy of V and run their
+    // first projection pass on it (see enqueue_level_kernels).
     Workspace(const DeviceOperator& op, const double* d_b, double regularization,
               int maximum_basis_size, cudaStream_t stream, bool time_operators,
-              bool use_graphs = true);
+              bool use_graphs = true, bool reduced_basis = false);
     ~Workspace();
     Workspace(const Workspace&) = delete;
     Workspace& operator=(const Workspace&) = delete;
@@ -99,6 +106,8 @@ public:
 
     // true once a level or seed wider than one column has been seen
     bool block_mode() const { return block_mode_; }
+    // whether width-one levels project on the FP32 copy of V
+    bool reduced_basis() const { return reduced_basis_; }
 
 private:
     void enqueue_level_kernels(cudaStream_t s, int pcap);
@@ -164,6 +173,16 @@ private:
     unsigned* counter_ = nullptr;   // self-resetting tickets: misc + one per V panel
 
     std::unique_ptr<PanelStore> V_;
+    // reduced-basis sweeps: FP32 copy of V, r rounded to FP32, the FP32
+    // coefficients, per-panel sums of c^2 and the tickets (panels | all)
+    bool reduced_basis_ = false;
+    std::unique_ptr<PanelStore32> V32_;
+    float* r32_ = nullptr;
+    float* c32_ = nullptr;
+    double* panel_sq_ = nullptr;
+    unsigned* red_tickets_ = nullptr;
+    double* red_part_ = nullptr;
+    int red_grid_ = 0;
     double* U_ = nullptr;      // m x ucap
     int ucap_ = 0;
     double* P_ = nullptr;      // m x pcap (pending seed)
@@ -246,5 +265,11 @@ private:
 // panel layout filled with a fixed pattern: `reps` launches of each, CUDA
 // events on `stream`; seconds[0] / seconds[1] receive the mean per launch.
 void probe_reorthogonalization(int n, int k, int reps, cudaStream_t stream, double seconds[2]);
+// The same for the reduced-basis sweeps (FP32 copy of V, FP32 products,
+// FP64 subtraction): seconds[0] / seconds[1] the V~^T r and r - V~ c passes;
+// max_rel_error[0] receives max |c - c_fp64| / ||r|| over the columns (the
+// projection's error against the FP64 sweep on the same basis).
+void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t stream,
+                                       double seconds[2], double* max_rel_error);
 
 }  // namespace amfls_gpu

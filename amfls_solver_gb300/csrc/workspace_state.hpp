@@ -58,7 +58,7 @@ struct DevState {
     int target_depth;     // depth at which the enqueued run of levels stops
     int iterations_left;  // hard cap on loop iterations of the enqueued run
     int sub_col;          // V column subtracted by the coupling (0 when none)
-    int pad_state;
+    int sweep_fp64;       // reduced-basis level: redo the projection in FP64
     // device time of search operator calls (globaltimer, ns)
     unsigned long long a_ns;
     unsigned long long at_ns;
@@ -70,6 +70,8 @@ struct DevState {
     long long search_a_calls;
     long long search_at_calls;
     long long levels_run;
+    long long reduced_levels;    // levels projected on the FP32 copy of V
+    long long reduced_fallbacks; // of those, levels redone in FP64
     // scalars of the current level
     double coupling;       // frontier coupling (1x1 at width one)
     double coupling_eff;   // coupling actually subtracted (0 when none applies)
