@@ -11,8 +11,8 @@
 //   d_k = argmin ||M~ d - s_k||   (AMFLS, lambda 0, on the reduced M~)
 //   x_{k+1} = x_k - d_k
 // until the FP64 certificate of x meets the tolerance, the certificate stops
-// shrinking (by a factor of two after a converged inner solve; at all after
-// an inner solve cut by maximum_depth), or the budget is spent.  With
+// shrinking (by a factor of two after a converged inner solve; at all within
+// two steps after inner solves cut by maximum_depth), or the budget is spent.  With
 // maximum_depth set and a tiny inner tolerance each inner solve is one
 // restart cycle of L = maximum_depth levels (restarted CG on the normal
 // equations, whose latest iterate minimises the energy-norm error over its
@@ -159,6 +159,7 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
     // iterate is the best correction in the energy norm
     io.latest_at_limit = true;
     double best = __builtin_huge_val();
+    double best_before_last = __builtin_huge_val();  // best certificate before the last step
     for (int k = 0; k < maximum_refinements; ++k) {
         io.stream = o.stream + (std::uint64_t)k;
         const SolveResult xr = solve_amfls(Ml, res, io, dx, stream);
@@ -201,10 +202,16 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
                                             cert});
         if (v.status == 0) break;
         // no longer contracting: an inner solve that converged (no depth
-        // limit) must halve the certificate; a restart cycle (stopped by
-        // maximum_depth) must still reduce it
+        // limit) must halve the certificate; restart cycles (stopped by
+        // maximum_depth) must reduce it within two cycles (restarted Krylov
+        // cycles often alternate a large and a small decrease)
         const bool cycle = xr.stop_reason == 3;
-        if (k > 0 && !(cert < (cycle ? 0.99 : 0.5) * best)) break;
+        if (cycle) {
+            if (k > 1 && !(cert < 0.99 * best_before_last)) break;
+        } else if (k > 0 && !(cert < 0.5 * best)) {
+            break;
+        }
+        best_before_last = best;
         best = std::min(best, cert);
         // s_{k+1} = M x_{k+1} - c in FP64 (A x - b, then sqrt(lambda) x)
         Epilogue ep;

@@ -25,7 +25,10 @@ roofline  the dominant kernels of the solve, the width-one
           size; algorithmic bytes 8 n k + 8 n (+ 8 n for the update);
 c3        time-to-tol on the 2,000,000 x 500,000 power-law CSR problem
           (lambda = 1e-4, tol = 1e-10; the metric's target workload): plain
-          FP64 and the chosen form, status, depth, certificate, time split;
+          FP64 and the chosen form (FP64 residual correction around restart
+          cycles with reduced-basis sweeps), status, depth, certificate, time
+          split, speed-up, x against plain FP64's, and the roofline of each
+          form's dominant sweeps;
 dense     the 100000 x 2000 column-major dense operator (lambda = 1e-6,
           tol = 1e-10): plain FP64 and the mixed form;
 spmm      CSR SpMM / SpMM^T GB/s (s = 1 and 8) on the 2M x 500k matrix;
@@ -64,6 +67,7 @@ import numpy as np  # noqa: E402
 METRIC = ("time-to-tol (s) mixed+batched+learned vs plain FP64 AMFLS on GB300; "
           "SpMM HBM GB/s")
 SEED = 20251203
+C3_CYCLE = 2000  # restart-cycle length of the chosen form on the 2M x 500k problem
 
 
 def parse():
@@ -240,6 +244,28 @@ def reorth_roofline(lib, n, k, stream, peak, peak_kind):
             "algorithmic_bytes": {"vt_r": bytes_vt, "v_c": bytes_vc}}
 
 
+def reduced_reorth_roofline(lib, n, k, stream, peak, peak_kind):
+    """The reduced-basis sweeps (FP32 copy of V: c = V~^T r~, r -= fl64(V~ c~))
+    timed live on `stream` at basis size k
+    (amfls_gpu_probe_reorthogonalization_reduced)."""
+    import ctypes
+    from amfls_solver_gb300 import _native
+    secs = (ctypes.c_double * 2)()
+    err = ctypes.c_double()
+    _native.check(lib.amfls_gpu_probe_reorthogonalization_reduced(
+        n, k, 50, ctypes.c_void_p(stream), secs, ctypes.byref(err)))
+    vt, vc = secs[0], secs[1]
+    bytes_vt = 4.0 * n * k + 4.0 * n * ((k + 31) // 32)  # V~ once, r~ once per panel
+    bytes_vc = 4.0 * n * k + 16.0 * n                    # V~ once, r in and out
+    achieved = (bytes_vt + bytes_vc) / (vt + vc) / 1e9
+    return {"kernel": "vt_r32_kernel (c = V~^T r~) + v_c32_kernel (r -= fl64(V~ c~))",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "basis_rows": n, "basis_cols": k, "launch_us": {"vt_r32": vt * 1e6, "v_c32": vc * 1e6},
+            "algorithmic_bytes": {"vt_r32": bytes_vt, "v_c32": bytes_vc},
+            "max_coefficient_error_rel_r": err.value}
+
+
 def spmm_measurement(dev, stream, peak):
     """CSR SpMM / SpMM^T HBM GB/s on the 2,000,000 x 500,000 power-law matrix,
     s = 1 and s = 8, through the C ABI on preallocated column-major device
@@ -331,6 +357,25 @@ def c3_measurement(dev):
         x_plain = plain.solution.clone()
         del plain
         torch.cuda.empty_cache()
+        # the chosen form: FP64 residual correction around restart cycles of
+        # C3_CYCLE levels whose first reorthogonalisation pass runs on an FP32
+        # copy of the basis (products, recurrence and validation in FP64)
+        mixed, t_mixed = timed_solve(lambda: amfls.run_amfls_mixed(
+            op, b, values="fp64", reduced_basis=True, inner_tolerance=1e-14,
+            maximum_refinements=40, maximum_depth=C3_CYCLE, **opts))
+        d = describe(mixed, t_mixed)
+        xm = mixed.solution
+        d.update({"form": (f"FP64 residual correction, restart cycles of {C3_CYCLE} levels, "
+                           "reduced-basis sweeps (FP32 copy of V, FP64 subtraction), FP64 "
+                           "operator products"),
+                  "cycles": int(mixed.trace_float.shape[0]),
+                  "cycle_certificates": [float(v) for v in mixed.trace_float[:, 17]],
+                  "reduced_basis_levels": mixed.reduced_basis_levels,
+                  "reduced_basis_fallbacks": mixed.reduced_basis_fallbacks,
+                  "x_rel_diff_vs_fp64": float(torch.linalg.norm(xm - x_plain) /
+                                              torch.linalg.norm(x_plain)),
+                  "speedup_vs_fp64": t_plain / t_mixed})
+        out["mixed"] = d
         return out, x_plain
     except Exception as e:  # reported, not fatal to the bench line
         return {"error": f"{type(e).__name__}: {e}"}, None
@@ -633,6 +678,10 @@ def run_ours(args, world, rank, local):
             if "fp64" in c3 and "depth" in c3["fp64"]:
                 c3["roofline"] = reorth_roofline(lib, c3["cols"], max(32, c3["fp64"]["depth"] // 2),
                                                  stream.cuda_stream, peak, peak_kind)
+            if "mixed" in c3:
+                c3["mixed"]["roofline"] = reduced_reorth_roofline(
+                    lib, c3["cols"], C3_CYCLE // 2, stream.cuda_stream, peak, peak_kind)
+                c3["mixed"]["roofline"]["note"] = "at the mean basis size of a restart cycle"
             legs["c3"] = c3
     if rank != 0:
         return
