@@ -18,6 +18,11 @@
 // equations, whose latest iterate minimises the energy-norm error over its
 // Krylov space): the basis, and so the cost of its sweeps, stays bounded by
 // L instead of growing with the whole solve.
+// When the reduced steps stop contracting (the levelling-off below) and the
+// reduced operator is not the FP64 one, the remaining steps run their inner
+// solves on the FP64 operator instead (a precision schedule), so the form
+// reaches what FP64 inner solves reach while the early steps use the cheaper
+// products.
 // Each step contracts the error by about cond(M) u_low + the inner
 // tolerance.  The inner AMFLS stops on a backward error relative to the
 // correction problem, whose residual tends to s* = M x* - c, so when s* is
@@ -138,9 +143,14 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
         }
     } release{{res, dx}};
 
-    std::unique_ptr<AugmentedOperator> aug_low;
+    // inner operators: M~ on the reduced operator, and M on the FP64 one
+    // for the steps after the reduced ones stop contracting
+    const bool escalate = &reduced != &op;
+    std::unique_ptr<AugmentedOperator> aug_low, aug_high;
     if (ridge) aug_low = std::make_unique<AugmentedOperator>(reduced, reg, stream);
-    const DeviceOperator& Ml = ridge ? static_cast<const DeviceOperator&>(*aug_low) : reduced;
+    if (ridge && escalate) aug_high = std::make_unique<AugmentedOperator>(op, reg, stream);
+    const DeviceOperator* Ml = ridge ? static_cast<const DeviceOperator*>(aug_low.get()) : &reduced;
+    bool fp64_inner = !escalate;
 
     Validator validator(op, d_b, reg, stream);
     SolveResult out;
@@ -162,7 +172,7 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
     double best_before_last = __builtin_huge_val();  // best certificate before the last step
     for (int k = 0; k < maximum_refinements; ++k) {
         io.stream = o.stream + (std::uint64_t)k;
-        const SolveResult xr = solve_amfls(Ml, res, io, dx, stream);
+        const SolveResult xr = solve_amfls(*Ml, res, io, dx, stream);
         accumulate(out.statistics, xr.statistics);
         out.depth += xr.depth;
         out.iterations += xr.iterations;
@@ -179,7 +189,7 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
         const double cert = certificate_of(v, reg);
         TraceRow row{};
         const double fr[29] = {
-            double(k), double(out.depth), double(out.auxiliary_width), double(xr.basis_rank),
+            double(k), double(out.depth), fp64_inner ? 1.0 : 0.0, double(xr.basis_rank),
             double(out.statistics.a_columns), double(out.statistics.at_columns),
             double(out.statistics.a_block_calls), double(out.statistics.at_block_calls),
             v.objective, v.residual_norm, v.augmented_residual_norm, v.normal_residual_norm,
@@ -206,13 +216,20 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
         // maximum_depth) must reduce it within two cycles (restarted Krylov
         // cycles often alternate a large and a small decrease)
         const bool cycle = xr.stop_reason == 3;
-        if (cycle) {
-            if (k > 1 && !(cert < 0.99 * best_before_last)) break;
-        } else if (k > 0 && !(cert < 0.5 * best)) {
-            break;
-        }
+        const bool stalled = cycle ? (k > 1 && !(cert < 0.99 * best_before_last))
+                                   : (k > 0 && !(cert < 0.5 * best));
         best_before_last = best;
         best = std::min(best, cert);
+        if (stalled) {
+            if (fp64_inner) break;
+            // precision schedule: the reduced products have contracted as
+            // far as they can; the remaining steps solve on the FP64
+            // operator (same restart cycles and sweeps)
+            fp64_inner = true;
+            Ml = ridge ? static_cast<const DeviceOperator*>(aug_high.get()) : &op;
+            best_before_last = __builtin_huge_val();
+            best = cert;
+        }
         // s_{k+1} = M x_{k+1} - c in FP64 (A x - b, then sqrt(lambda) x)
         Epilogue ep;
         ep.out = res;

@@ -229,11 +229,21 @@ int amfls_gpu_reduced_operator_create(const amfls_gpu_operator* source, int valu
  * inner_tolerance on `reduced` (lambda = 0) or on [reduced; sqrt(lambda) I]
  * (lambda > 0) for the correction of the current x, then validates x with
  * the certified FP64 validation on `op`.  It stops when that certificate
- * meets options->tolerance (status 0), when it no longer halves, or after
- * maximum_refinements steps.  result->status / stop_reason and the metrics
- * are those of the last FP64 validation; depth and iterations add up the
- * inner solves; one trace row per outer step (column 0 the step, column 3
- * the inner basis rank).  Same buffer conventions as amfls_gpu_solve_amfls. */
+ * meets options->tolerance (status 0), when it no longer contracts, or after
+ * maximum_refinements steps.  It no longer contracts when it fails to halve
+ * after an inner solve that reached inner_tolerance, or, for inner solves
+ * cut by options->maximum_depth (restart cycles: pass a tiny
+ * inner_tolerance and the cycle length as maximum_depth), when it fails to
+ * fall below 0.99 of its best value two steps earlier.  When the steps on
+ * `reduced` stop contracting and `reduced` is not `op`, the remaining steps
+ * solve on `op` instead (precision schedule); `reduced` == `op` runs FP64
+ * inner solves throughout.  options->reduced_basis applies to the inner
+ * solves.  result->status / stop_reason and the metrics are those of the
+ * last FP64 validation; depth and iterations add up the inner solves; one
+ * trace row per outer step (column 0 the step, column 1 the levels so far,
+ * column 2 1 when the step solved on `op`, column 3 the inner basis rank,
+ * column 17 the step's relative energy error bound).  Same buffer
+ * conventions as amfls_gpu_solve_amfls. */
 int amfls_gpu_solve_amfls_mixed(const amfls_gpu_operator* op, const amfls_gpu_operator* reduced,
                                 const double* d_b, const amfls_gpu_options* options,
                                 double inner_tolerance, int maximum_refinements,
