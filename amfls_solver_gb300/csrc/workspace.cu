@@ -344,8 +344,11 @@ vt_r_kernel(double* const* __restrict__ panels, int n, int chunk_rows,
     }
 }
 
-// out = r - V c (subtract) or out = V c; 32 rows per block, warps split the
-// panels.  Sum of squares of out reduced by the last block, then `hook`.
+// out = r - V c (subtract) or out = V c; 32-row tiles, warps split the
+// panels; a block takes tiles blockIdx.x, blockIdx.x + gridDim.x, ... (one
+// tile per block when the grid covers them, fewer blocks for launches that
+// usually find their guard off).  Sum of squares of out reduced by the last
+// block, then `hook`.
 // guarded: 0 always runs, 1 runs when the level (and pass) runs, 2 as 1 but
 // only when a reduced-basis level redoes its projection in FP64.
 __global__ void __launch_bounds__(kThreads)
@@ -358,60 +361,64 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
     const int k = k_arg >= 0 ? k_arg : st->k;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int q = lane & 3, rsub = lane >> 2;
-    const long long row0 = (long long)blockIdx.x * 32;
     const int P = (k + 31) / 32;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int p = warp; p < P; p += 8) {
-        const double* __restrict__ vp = panels[p];
-        double cv[8];
+    const long long tiles = ((long long)n + 31) / 32;
+    __shared__ double sm[8][32];
+    __shared__ double red[32];
+    double sq = 0.0;
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const long long row0 = tile * 32;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int p = warp; p < P; p += 8) {
+            const double* __restrict__ vp = panels[p];
+            double cv[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int col = p * 32 + q * 8 + i;
-            cv[i] = col < k ? c[col] : 0.0;
+            for (int i = 0; i < 8; ++i) {
+                const int col = p * 32 + q * 8 + i;
+                cv[i] = col < k ? c[col] : 0.0;
+            }
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                const long long row = row0 + s * 8 + rsub;
+                if (row < n) {
+                    const double2* src = reinterpret_cast<const double2*>(vp + row * 32 + q * 8);
+                    const double2 a0 = __ldg(src), a1 = __ldg(src + 1), a2 = __ldg(src + 2),
+                                  a3 = __ldg(src + 3);
+                    double t = acc[s];
+                    t = fma(a0.x, cv[0], t);
+                    t = fma(a0.y, cv[1], t);
+                    t = fma(a1.x, cv[2], t);
+                    t = fma(a1.y, cv[3], t);
+                    t = fma(a2.x, cv[4], t);
+                    t = fma(a2.y, cv[5], t);
+                    t = fma(a3.x, cv[6], t);
+                    t = fma(a3.y, cv[7], t);
+                    acc[s] = t;
+                }
+            }
         }
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const long long row = row0 + s * 8 + rsub;
+            acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 1);
+            acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 2);
+        }
+        if (q == 0) {
+#pragma unroll
+            for (int s = 0; s < 4; ++s) sm[warp][s * 8 + rsub] = acc[s];
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const long long row = row0 + threadIdx.x;
+            double y = 0.0;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) y += sm[w][threadIdx.x];
             if (row < n) {
-                const double2* src = reinterpret_cast<const double2*>(vp + row * 32 + q * 8);
-                const double2 a0 = __ldg(src), a1 = __ldg(src + 1), a2 = __ldg(src + 2),
-                              a3 = __ldg(src + 3);
-                double t = acc[s];
-                t = fma(a0.x, cv[0], t);
-                t = fma(a0.y, cv[1], t);
-                t = fma(a1.x, cv[2], t);
-                t = fma(a1.y, cv[3], t);
-                t = fma(a2.x, cv[4], t);
-                t = fma(a2.y, cv[5], t);
-                t = fma(a3.x, cv[6], t);
-                t = fma(a3.y, cv[7], t);
-                acc[s] = t;
+                const double o = subtract ? r_in[row] - y : y;
+                out[row] = o;
+                sq = fma(o, o, sq);
             }
         }
-    }
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-        acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 1);
-        acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 2);
-    }
-    __shared__ double sm[8][32];
-    __shared__ double red[32];
-    if (q == 0) {
-#pragma unroll
-        for (int s = 0; s < 4; ++s) sm[warp][s * 8 + rsub] = acc[s];
-    }
-    __syncthreads();
-    double sq = 0.0;
-    if (threadIdx.x < 32) {
-        const long long row = row0 + threadIdx.x;
-        double y = 0.0;
-#pragma unroll
-        for (int w = 0; w < 8; ++w) y += sm[w][threadIdx.x];
-        if (row < n) {
-            const double o = subtract ? r_in[row] - y : y;
-            out[row] = o;
-            sq = o * o;
-        }
+        __syncthreads();  // sm is reused by the next tile
     }
     if (hook == kHookNone) return;
     const double bs = block_sum(sq, red);
@@ -1415,6 +1422,9 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     const int chunks = std::max(1, std::min(max_chunks, (gemv_target_blocks() + pcap - 1) / pcap));
     const int chunk_rows = (int)(((long long)n_ + chunks - 1) / chunks);
     const bool reduced = reduced_basis_ && !block_mode_;
+    // grid of the sweeps that usually find their guard off (DGKS second
+    // pass, FP64 redo of a reduced pass): a few blocks per SM
+    const int rare_grid = (int)std::min<long long>(tiles, 2LL * sm_count());
     if (reduced) {
         // first pass on the FP32 copy of V; the FP64 kernels after it run
         // only when the coefficients were too large for it (sweep_fp64)
@@ -1433,7 +1443,7 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
                                                      partials_ + vc_partials_offset_, counter_ + 3,
                                                      dstate_, m_);
         AMFLS_LAUNCHED();
-        v_c_kernel<<<(int)tiles, kThreads, 0, s>>>(
+        v_c_kernel<<<rare_grid, kThreads, 0, s>>>(
             V_->device_table(), n_, -1, c1_, R_, R_, 1, partials_ + vc_partials_offset_,
             counter_ + 3, dstate_, kHookRightPass1, m_, 2, 1);
         AMFLS_LAUNCHED();
@@ -1455,7 +1465,8 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
                                                                 R_, c, partials_, counter_ + 64,
                                                                 dstate_, pass);
             AMFLS_LAUNCHED();
-            v_c_kernel<<<(int)tiles, kThreads, 0, s>>>(
+            // the second pass rarely runs: a grid that is cheap to skip
+            v_c_kernel<<<pass == 1 ? (int)tiles : rare_grid, kThreads, 0, s>>>(
                 V_->device_table(), n_, -1, c, R_, R_, 1, partials_ + vc_partials_offset_,
                 counter_ + 3, dstate_, hook, m_, 1, pass);
             AMFLS_LAUNCHED();
