@@ -307,14 +307,16 @@ class DeviceOperator:
         return y.reshape(-1) if vec else y
 
     def tile_schedule(self):
-        """CSR operators: ({"A": "chains" | "row blocks", "A^T": ...}, timings
-        in microseconds {(side, tiling): us} of the construction-time
-        autotuner, empty where it did not run)."""
+        """CSR operators: ({"A": "row vector" | "chains" | "row blocks",
+        "A^T": ...}, timings in microseconds {(side, tiling): us} of the
+        construction-time autotuner's tile candidates, empty where it did not
+        run)."""
         chains = (ctypes.c_int * 2)()
         us = (ctypes.c_double * 4)()
         _native.check(_native.load().amfls_gpu_csr_operator_schedule(self.handle, chains, us))
         names = ("A", "A^T")
-        choice = {names[i]: "chains" if chains[i] else "row blocks" for i in range(2)}
+        kinds = {0: "row blocks", 1: "chains", 2: "row vector"}
+        choice = {names[i]: kinds[int(chains[i])] for i in range(2)}
         times = {f"{names[i // 2]} {'chains' if i % 2 else 'row blocks'}": us[i]
                  for i in range(4) if us[i] > 0}
         return choice, times

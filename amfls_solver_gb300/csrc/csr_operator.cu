@@ -37,6 +37,7 @@
 #include "common.cuh"
 #include "csr_operator.hpp"
 #include "csr_tiles.cuh"
+#include "csr_vector.cuh"
 #include "dd.cuh"
 #include "epilogue.cuh"
 #include "fp_bounds.cuh"
@@ -517,6 +518,33 @@ void launch_tiles(const int* off, const int* idx, const V* val, const TileStore&
                                       stream);
 }
 
+// Resident grid of the row-vector kernel, at most the blocks its warp tasks
+// need and max_blocks().
+template <typename V>
+int vector_grid(long long warp_tasks) {
+    static const int resident = [] {
+        int dev = 0, nb = 0, sms = 0;
+        AMFLS_CUDA(cudaGetDevice(&dev));
+        AMFLS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, csr_vector::vector_product_kernel<V>, csr_vector::kThreads, 0));
+        return std::max(1, nb) * sms;
+    }();
+    const long long need = (warp_tasks + csr_vector::kWarps - 1) / csr_vector::kWarps;
+    return (int)std::max<long long>(1, std::min<long long>({need, (long long)resident,
+                                                            (long long)max_blocks()}));
+}
+
+template <typename V>
+void launch_vector(const int* off, const int* idx, const V* val, const csr_vector::Table& vt,
+                   const double* x, const Epilogue& ep, double* partials, unsigned* counter,
+                   cudaStream_t stream) {
+    const int grid = vector_grid<V>(vt.warp_start[csr_vector::kBins]);
+    csr_vector::vector_product_kernel<V><<<grid, csr_vector::kThreads, 0, stream>>>(
+        off, idx, val, vt, x, ep, partials, counter);
+    AMFLS_LAUNCHED();
+}
+
 }  // namespace
 
 // Autotuning of the single-column tiling: sides with at least this many
@@ -537,6 +565,12 @@ struct CsrOperator::Side {
     TileStore one;             // single-column products: chain groups or row blocks, long rows
     TileStore many;            // row blocks of kEC elements: 2..8 columns
     double tuned_us[2] = {0.0, 0.0};  // measured product time: row blocks, chain groups
+    // row-vector single-column products (csr_vector.cuh): rows by bin and
+    // length, used instead of `one` when `vector` is set
+    int* vrows = nullptr;
+    csr_vector::Table vtab{};
+    bool vector = false;
+    double vector_us = 0.0;
 };
 
 namespace {
@@ -564,6 +598,58 @@ double time_tiles(const int* off32, const int* idx, const double* val, const Til
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return 1e3 * ms / reps;
+}
+
+// The same for the row-vector kernel.
+double time_vector(const int* off32, const int* idx, const double* val,
+                   const csr_vector::Table& vt, const double* x, double* y, double* scratch,
+                   unsigned* counter, cudaStream_t stream) {
+    Epilogue ep;
+    ep.out = y;
+    cudaEvent_t e0, e1;
+    AMFLS_CUDA(cudaEventCreate(&e0));
+    AMFLS_CUDA(cudaEventCreate(&e1));
+    constexpr int reps = 5;
+    for (int i = 0; i < 2; ++i) launch_vector(off32, idx, val, vt, x, ep, scratch, counter, stream);
+    AMFLS_CUDA(cudaEventRecord(e0, stream));
+    for (int i = 0; i < reps; ++i) launch_vector(off32, idx, val, vt, x, ep, scratch, counter, stream);
+    AMFLS_CUDA(cudaEventRecord(e1, stream));
+    AMFLS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    AMFLS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return 1e3 * ms / reps;
+}
+
+// Row order and bin boundaries of the row-vector kernel: rows by bin
+// (descending lanes per row), longest first within a bin, ties in row order.
+void make_vector_table(const std::vector<long long>& host_off, int count, int** d_rows,
+                       csr_vector::Table& vt, cudaStream_t stream) {
+    std::vector<int> order(std::max(1, count));
+    std::vector<int> bin(count);
+    int counts[csr_vector::kBins] = {};
+    for (int r = 0; r < count; ++r) {
+        bin[r] = csr_vector::bin_of(host_off[r + 1] - host_off[r]);
+        ++counts[bin[r]];
+    }
+    std::iota(order.begin(), order.begin() + count, 0);
+    std::stable_sort(order.begin(), order.begin() + count, [&](int a, int b) {
+        if (bin[a] != bin[b]) return bin[a] < bin[b];
+        return host_off[a + 1] - host_off[a] > host_off[b + 1] - host_off[b];
+    });
+    vt.row_start[0] = 0;
+    vt.warp_start[0] = 0;
+    for (int b = 0; b < csr_vector::kBins; ++b) {
+        vt.row_start[b + 1] = vt.row_start[b] + counts[b];
+        const long long per_warp = 1LL << b;
+        vt.warp_start[b + 1] = vt.warp_start[b] + (counts[b] + per_warp - 1) / per_warp;
+    }
+    AMFLS_CUDA(cudaMalloc(d_rows, sizeof(int) * std::max(1, count)));
+    AMFLS_CUDA(cudaMemcpyAsync(*d_rows, order.data(), sizeof(int) * std::max(1, count),
+                               cudaMemcpyHostToDevice, stream));
+    AMFLS_CUDA(cudaStreamSynchronize(stream));  // `order` goes out of scope
+    vt.rows = *d_rows;
 }
 
 }  // namespace
@@ -605,6 +691,8 @@ void CsrOperator::release() {
         s->off32 = nullptr;
         s->one.release();
         s->many.release();
+        cudaFree(s->vrows);
+        s->vrows = nullptr;
     }
     cudaFree(scratch_);
     scratch_ = nullptr;
@@ -843,11 +931,16 @@ void CsrOperator::fill_ids(int* ids, long long n, cudaStream_t stream) {
 
 namespace {
 
-// Single-column product of one side with a fused epilogue.
+// Single-column product of one side with a fused epilogue: the row-vector
+// kernel when the side's autotuner chose it (vt non-null), else the tiles.
 template <typename V>
 void side_product1(const int* off32, const int* idx, const V* vals, const TileStore& one,
                    const double* x, const Epilogue& ep, double* partials, unsigned* counter,
-                   cudaStream_t stream) {
+                   cudaStream_t stream, const csr_vector::Table* vt = nullptr) {
+    if (vt) {
+        launch_vector(off32, idx, vals, *vt, x, ep, partials, counter, stream);
+        return;
+    }
     launch_tiles<1, true>(off32, idx, vals, one, x, nullptr, 0, 1, ep, partials, counter, stream);
 }
 
@@ -857,7 +950,7 @@ template <typename V>
 void side_block(const int* off32, const int* idx, const V* vals, const TileStore& one,
                 const TileStore& many, const double* x, long long ldx, int block_cols,
                 double* y, long long ldy, double* xrows, double* partials, unsigned* counter,
-                cudaStream_t stream) {
+                cudaStream_t stream, const csr_vector::Table* vt = nullptr) {
     const Epilogue none;
     const int tgrid = setup_grid(ldx);
     for (int c0 = 0; c0 < block_cols; c0 += 8) {
@@ -882,7 +975,7 @@ void side_block(const int* off32, const int* idx, const V* vals, const TileStore
         } else {
             Epilogue ep;
             ep.out = yc;
-            side_product1(off32, idx, vals, one, xc, ep, partials, counter, stream);
+            side_product1(off32, idx, vals, one, xc, ep, partials, counter, stream, vt);
         }
     }
 }
@@ -906,6 +999,12 @@ __global__ void narrow_values_kernel(const double* in, long long n, V* out) {
 // least kTuneMargin.  AMFLS_GB300_CSR_CHAINS (either value) turns it off.
 void CsrOperator::tune_single_column(Side& sd, const std::vector<long long>& host_off,
                                      cudaStream_t stream) {
+    const char* force_vector = std::getenv("AMFLS_GB300_CSR_VECTOR");
+    if (force_vector && force_vector[0] == '1' && sd.count > 0) {
+        make_vector_table(host_off, sd.count, &sd.vrows, sd.vtab, stream);
+        sd.vector = true;
+        return;
+    }
     if (std::getenv("AMFLS_GB300_CSR_CHAINS") || sd.count <= 0 ||
         host_off[sd.count] < kTuneMinNonzeros)
         return;
@@ -920,19 +1019,38 @@ void CsrOperator::tune_single_column(Side& sd, const std::vector<long long>& hos
                                      stream);
     const double t_alt = time_tiles(sd.off32, sd.idx, sd.val, alt, x, y, scratch_, counter_,
                                     stream);
+    // the row-vector kernel is the third candidate (AMFLS_GB300_CSR_VECTOR=0
+    // leaves it out)
+    double t_vec = 0.0;
+    if (!(force_vector && force_vector[0] == '0')) {
+        make_vector_table(host_off, sd.count, &sd.vrows, sd.vtab, stream);
+        t_vec = time_vector(sd.off32, sd.idx, sd.val, sd.vtab, x, y, scratch_, counter_, stream);
+    }
     AMFLS_CUDA(cudaFreeAsync(x, stream));
     AMFLS_CUDA(cudaFreeAsync(y, stream));
     AMFLS_CUDA(cudaStreamSynchronize(stream));
     sd.tuned_us[sd.one.chains ? 1 : 0] = t_rule;
     sd.tuned_us[alt.chains ? 1 : 0] = t_alt;
-    if (t_alt < (1.0 - kTuneMargin) * t_rule) std::swap(sd.one, alt);
+    sd.vector_us = t_vec;
+    double best = t_rule;
+    if (t_alt < (1.0 - kTuneMargin) * t_rule) {
+        std::swap(sd.one, alt);
+        best = t_alt;
+    }
     alt.release();
+    if (sd.vrows && t_vec < (1.0 - kTuneMargin) * best) {
+        sd.vector = true;
+    } else if (sd.vrows) {
+        cudaFree(sd.vrows);
+        sd.vrows = nullptr;
+        sd.vtab = csr_vector::Table{};
+    }
 }
 
 void CsrOperator::single_column_schedule(int chains[2], double microseconds[4]) const {
     const Side* sides[2] = {a_.get(), t_.get()};
     for (int i = 0; i < 2; ++i) {
-        chains[i] = sides[i]->one.chains ? 1 : 0;
+        chains[i] = sides[i]->vector ? 2 : (sides[i]->one.chains ? 1 : 0);
         microseconds[2 * i] = sides[i]->tuned_us[0];
         microseconds[2 * i + 1] = sides[i]->tuned_us[1];
     }
@@ -942,7 +1060,7 @@ bool CsrOperator::product1(bool transpose, const double* x, const Epilogue& ep,
                            cudaStream_t stream) const {
     const Side& s = transpose ? *t_ : *a_;
     side_product1(s.off32, s.idx, s.val, s.one, x, ep, ep.partials ? ep.partials : scratch_,
-                  ep.counter ? ep.counter : counter_, stream);
+                  ep.counter ? ep.counter : counter_, stream, s.vector ? &s.vtab : nullptr);
     return true;
 }
 
@@ -952,7 +1070,8 @@ void CsrOperator::product(bool transpose, const double* x, int block_cols, doubl
         throw std::invalid_argument("CSR product block is invalid");
     const Side& s = transpose ? *t_ : *a_;
     side_block(s.off32, s.idx, s.val, s.one, s.many, x, transpose ? rows_ : cols_, block_cols, y,
-               transpose ? cols_ : rows_, xrows_, scratch_, counter_, stream);
+               transpose ? cols_ : rows_, xrows_, scratch_, counter_, stream,
+               s.vector ? &s.vtab : nullptr);
 }
 
 // ------------------------------------------------- reduced precision ----
@@ -1011,12 +1130,13 @@ bool ReducedCsrOperator::product1(bool transpose, const double* x, const Epilogu
     double* partials = ep.partials ? ep.partials : scratch_;
     unsigned* counter = ep.counter ? ep.counter : counter_;
     const void* v = vals_[transpose ? 1 : 0];
+    const csr_vector::Table* vt = s.vector ? &s.vtab : nullptr;
     if (type_ == ValueType::fp32)
         side_product1(s.off32, s.idx, static_cast<const float*>(v), s.one, x, ep, partials,
-                      counter, stream);
+                      counter, stream, vt);
     else
         side_product1(s.off32, s.idx, static_cast<const __nv_bfloat16*>(v), s.one, x, ep,
-                      partials, counter, stream);
+                      partials, counter, stream, vt);
     return true;
 }
 
@@ -1028,12 +1148,13 @@ void ReducedCsrOperator::product(bool transpose, const double* x, int block_cols
     const long long ldx = transpose ? src_.rows_ : src_.cols_;
     const long long ldy = transpose ? src_.cols_ : src_.rows_;
     const void* v = vals_[transpose ? 1 : 0];
+    const csr_vector::Table* vt = s.vector ? &s.vtab : nullptr;
     if (type_ == ValueType::fp32)
         side_block(s.off32, s.idx, static_cast<const float*>(v), s.one, s.many, x, ldx,
-                   block_cols, y, ldy, xrows_, scratch_, counter_, stream);
+                   block_cols, y, ldy, xrows_, scratch_, counter_, stream, vt);
     else
         side_block(s.off32, s.idx, static_cast<const __nv_bfloat16*>(v), s.one, s.many, x, ldx,
-                   block_cols, y, ldy, xrows_, scratch_, counter_, stream);
+                   block_cols, y, ldy, xrows_, scratch_, counter_, stream, vt);
 }
 
 void ReducedCsrOperator::apply(const double* x, int block_cols, double* y, cudaStream_t s) const {

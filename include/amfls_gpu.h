@@ -345,11 +345,15 @@ int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, void* st
  * 203-269).  A side (A, or the stored transpose) is cut into warp tasks
  * either as chain groups or as row blocks; sides of at least 2^18 nonzeros
  * time both tilings when the operator is created and keep the faster one
- * when it wins by at least 10% over the size / row-length rule's choice.
- * chains[0], chains[1]: 1 when A's / the transpose's products use chain
- * groups; microseconds[0..3]: the timed products of A with row blocks and
- * with chain groups, then the transpose's (0 where not timed).  An operator
- * that is not a CSR operator is AMFLS_GPU_INVALID_ARGUMENT. */
+ * when it wins by at least 10% over the size / row-length rule's choice; the
+ * row-vector kernel (rows binned by length, 1-32 lanes per row, no shared
+ * memory) is timed as a third candidate and replaces the tiles when it beats
+ * the kept tiling by 10%.
+ * chains[0], chains[1]: 0 when A's / the transpose's products use row
+ * blocks, 1 chain groups, 2 the row-vector kernel; microseconds[0..3]: the
+ * timed products of A with row blocks and with chain groups, then the
+ * transpose's (0 where not timed).  An operator that is not a CSR operator
+ * is AMFLS_GPU_INVALID_ARGUMENT. */
 int amfls_gpu_csr_operator_schedule(const amfls_gpu_operator* op, int* chains,
                                     double* microseconds);
 
