@@ -35,33 +35,99 @@ __device__ __forceinline__ void epilogue_row(const Epilogue& ep, int row, double
     }
 }
 
+// Maximum / sum over a block of 64-bit integers (warp shuffles, then warp 0),
+// valid in warp 0.  Integer pipes: the FP64 pipe of this GPU is scarce.
+__device__ inline unsigned long long block_umax(unsigned long long v, unsigned long long* sc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sc[warp] = v;
+    __syncthreads();
+    unsigned long long r = 0;
+    if (warp == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sc[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_xor_sync(0xffffffffu, r, o);
+            r = w > r ? w : r;
+        }
+    }
+    return r;
+}
+
+__device__ inline unsigned long long block_usum(unsigned long long v, unsigned long long* sc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sc[warp] = v;
+    __syncthreads();
+    unsigned long long r = 0;
+    if (warp == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sc[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    return r;
+}
+
+// Cross-block reduction of the epilogue terms into *ep.red.  The sums run on
+// the FP64 pipe in a fixed tree; the maxima (non-negative magnitudes, so
+// their bit patterns order like their values) and the non-finite count run
+// on the integer pipes, with the results fmax / a count would give.  Per
+// block: 6 slots of `partials` (maxima and count stored as bit patterns).
 __device__ inline void finish_reduction(const Epilogue& ep, double sq_t, double sq_out, double dot,
                                  double mx_t, double mx_out, int nonfin, double* partials,
                                  unsigned* counter) {
     __shared__ double scratch[32];
+    __shared__ unsigned long long uscratch[32];
     if (!ep.red) return;
-    double v[6] = {sq_t, sq_out, dot, mx_t, mx_out, (double)nonfin};
-    double r[6];
-    for (int i = 0; i < 6; ++i)
-        r[i] = (i == 3 || i == 4) ? block_max(v[i], scratch) : block_sum(v[i], scratch);
-    if (threadIdx.x == 0)
-        for (int i = 0; i < 6; ++i) partials[blockIdx.x * 6 + i] = r[i];
+    const double s0 = block_sum(sq_t, scratch);
+    const double s1 = block_sum(sq_out, scratch);
+    const double s2 = block_sum(dot, scratch);
+    const unsigned long long m3 = block_umax(__double_as_longlong(mx_t), uscratch);
+    const unsigned long long m4 = block_umax(__double_as_longlong(mx_out), uscratch);
+    const unsigned long long c5 = block_usum((unsigned long long)nonfin, uscratch);
+    if (threadIdx.x == 0) {
+        double* p = partials + blockIdx.x * 6;
+        p[0] = s0;
+        p[1] = s1;
+        p[2] = s2;
+        p[3] = __longlong_as_double(m3);
+        p[4] = __longlong_as_double(m4);
+        p[5] = __longlong_as_double(c5);
+    }
     if (arrive_last(counter, gridDim.x)) {
-        for (int i = 0; i < 6; ++i) {
-            double a = (i == 3 || i == 4) ? 0.0 : 0.0;
-            for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-                const double p = partials[b * 6 + i];
-                a = (i == 3 || i == 4) ? fmax(a, p) : a + p;
-            }
-            r[i] = (i == 3 || i == 4) ? block_max(a, scratch) : block_sum(a, scratch);
+        double a[3] = {0.0, 0.0, 0.0};
+        unsigned long long mx[2] = {0ull, 0ull}, cnt = 0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+            const double* p = partials + b * 6;
+            a[0] += p[0];
+            a[1] += p[1];
+            a[2] += p[2];
+            const unsigned long long x3 = __double_as_longlong(p[3]);
+            const unsigned long long x4 = __double_as_longlong(p[4]);
+            mx[0] = x3 > mx[0] ? x3 : mx[0];
+            mx[1] = x4 > mx[1] ? x4 : mx[1];
+            cnt += __double_as_longlong(p[5]);
         }
+        const double r0 = block_sum(a[0], scratch);
+        const double r1 = block_sum(a[1], scratch);
+        const double r2 = block_sum(a[2], scratch);
+        const unsigned long long r3 = block_umax(mx[0], uscratch);
+        const unsigned long long r4 = block_umax(mx[1], uscratch);
+        const unsigned long long r5 = block_usum(cnt, uscratch);
         if (threadIdx.x == 0) {
-            ep.red->sq_t = r[0];
-            ep.red->sq_out = r[1];
-            ep.red->dot = r[2];
-            ep.red->max_t = r[3];
-            ep.red->max_out = r[4];
-            ep.red->nonfinite = (int)r[5];
+            ep.red->sq_t = r0;
+            ep.red->sq_out = r1;
+            ep.red->dot = r2;
+            ep.red->max_t = __longlong_as_double(r3);
+            ep.red->max_out = __longlong_as_double(r4);
+            ep.red->nonfinite = (int)r5;
         }
     }
 }

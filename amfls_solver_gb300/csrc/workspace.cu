@@ -1489,9 +1489,10 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     op_.product1(false, vnew_, el, s);
     const int lgrid = (int)std::max<long long>(1, std::min<long long>(grid_cap(), (m_ + 1023) / 1024));
     for (int pass = 1; pass <= 2; ++pass) {
-        left_pass_kernel<<<lgrid, kThreads, 0, s>>>(Y_, U_, b_, m_, &red_[1], partials_,
-                                                    counter_ + 4, dstate_, pass, n_, alpha_, beta_,
-                                                    g_);
+        // the second pass rarely runs: a grid that is cheap to skip
+        left_pass_kernel<<<pass == 1 ? lgrid : std::min(lgrid, rare_grid), kThreads, 0, s>>>(
+            Y_, U_, b_, m_, &red_[1], partials_, counter_ + 4, dstate_, pass, n_, alpha_, beta_,
+            g_);
         AMFLS_LAUNCHED();
     }
     normalize_left_kernel<<<(int)std::min<long long>(grid_cap(), (m_ + 255) / 256), 256, 0, s>>>(
