@@ -1674,7 +1674,14 @@ void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, d
     stream_alloc(&c, sizeof(double) * 32 * P, s);
     stream_alloc(&c64, sizeof(double) * 32 * P, s);
     stream_alloc(&c32, sizeof(float) * 32 * P, s);
-    stream_alloc(&part, sizeof(double) * reduced_part_doubles(grid, P), s);
+    // partial sums of the reduced pass ([P][chunks][32], reduced_chunks) and
+    // of the FP64 reference pass ([P][chunks64][32]) share one buffer
+    const int chunks64 = std::max(1, std::min((int)std::max<long long>(1, (n + 255) / 256),
+                                              (gemv_target_blocks() + P - 1) / P));
+    stream_alloc(&part,
+                 sizeof(double) * std::max<long long>(reduced_part_doubles(grid, P),
+                                                      32LL * P * chunks64),
+                 s);
     stream_alloc(&psq, sizeof(double) * P, s);
     stream_alloc(&vcpart, sizeof(double) * (tiles + 1), s);
     stream_alloc(&tickets, sizeof(unsigned) * (2 * P + 2), s);
@@ -1696,11 +1703,9 @@ void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, d
     AMFLS_LAUNCHED();
     // the FP64 projection of the same basis, for the error
     {
-        const int chunks = std::max(1, std::min((int)std::max<long long>(1, (n + 255) / 256),
-                                                (gemv_target_blocks() + P - 1) / P));
-        const int chunk_rows = (int)(((long long)n + chunks - 1) / chunks);
-        vt_r_kernel<<<dim3(P, chunks), kThreads, 0, s>>>(V.device_table(), n, chunk_rows, r, c64,
-                                                         part, tickets, st, 1);
+        const int chunk_rows = (int)(((long long)n + chunks64 - 1) / chunks64);
+        vt_r_kernel<<<dim3(P, chunks64), kThreads, 0, s>>>(V.device_table(), n, chunk_rows, r,
+                                                           c64, part, tickets, st, 1);
         AMFLS_LAUNCHED();
     }
     auto vt = [&] {
