@@ -189,6 +189,11 @@ def replays():
     replay_fixture("replay_csr_ls_forced",
                    ("portable_csr", dict(m=2000, n=500, seed=1)),
                    regularization=0.0, tolerance=1e-8, seed=7, replay=[0, 1, 1, 0, 1] + [0] * 64)
+    # a tall ridge problem for the mixed form's comparison with the reference
+    # (the 2,000,000 x 500,000 problem is out of the reference's reach)
+    replay_fixture("replay_csr_ridge_60000x15000",
+                   ("portable_csr", dict(m=60000, n=15000, per_row=10, octaves=20, seed=3)),
+                   regularization=1e-4, tolerance=1e-10)
 
 
 def main():

@@ -101,3 +101,35 @@ def test_restarted_ridge_solve_with_and_without_reduced_basis(amfls):
     ref = runs[False, 1000]
     for key in ((True, 1000), (True, 500)):
         assert np.linalg.norm(runs[key] - ref) <= 4 * tol * cond * np.linalg.norm(ref)
+
+
+def test_mixed_form_against_the_reference_on_a_tall_ridge_problem(amfls):
+    """The chosen form against the reference's own solve of a 60000 x 15000
+    portable CSR ridge problem (lambda = 1e-4, tol 1e-10; the reference
+    certified it in 2560 levels): restart cycles of 1000 levels with
+    reduced-basis sweeps certify the tolerance, and x agrees with the
+    reference's x to 2.5 tol in the energy norm ||v||_H^2 = ||A v||^2 +
+    lambda ||v||^2 (both x lie within tol of the exact solution there) and
+    to 2 tol ||M|| / sqrt(lambda) relative in the 2-norm."""
+    import scipy.sparse as sp
+    from conftest import golden_options, load_replay
+
+    data, prob = load_replay("replay_csr_ridge_60000x15000")
+    opts = golden_options(data)
+    reg, tol = opts["regularization"], opts["tolerance"]
+    op = amfls.DeviceOperator(_csr(prob))
+    r = amfls.run_amfls_mixed(op, torch.from_numpy(prob.b).cuda(), values="fp64",
+                              reduced_basis=True, inner_tolerance=1e-14, maximum_refinements=60,
+                              maximum_depth=1000, regularization=reg, tolerance=tol)
+    assert r.status == 0 and r.relative_energy_error_upper_bound <= tol
+    assert r.reduced_basis_levels > 0
+    a = sp.csr_matrix((prob.values, prob.column_indices, prob.row_offsets),
+                      shape=(prob.rows, prob.cols))
+    hnorm = lambda v: np.sqrt(np.linalg.norm(a @ v) ** 2 + reg * np.linalg.norm(v) ** 2)
+    x, xr = r.solution.cpu().numpy(), data["solution"]
+    assert hnorm(x - xr) <= 2.5 * tol * hnorm(xr)
+    norm_m = np.sqrt(op.validation_error_model()[0] ** 2 + reg)
+    rel = np.linalg.norm(x - xr) / np.linalg.norm(xr)
+    print(f"\nmixed form vs reference: {r.depth} levels ({int(r.trace_float.shape[0])} cycles), "
+          f"x relative difference {rel:.2e}, energy norm {hnorm(x - xr) / hnorm(xr):.2e}")
+    assert rel <= 2 * tol * norm_m / np.sqrt(reg)

