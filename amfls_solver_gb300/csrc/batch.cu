@@ -5,10 +5,16 @@
 // A pool of host worker threads, each with its own non-blocking CUDA
 // stream, takes problems from a shared queue ordered by estimated cost
 // (largest first, the LPT rule, so the last problems to start are the
-// short ones).  Every solve runs its width-one levels as CUDA graphs on its
-// worker's stream, so the GPU interleaves the levels of up to `workers`
-// problems; small problems, whose levels are launch- and latency-bound,
-// share the SMs instead of leaving them idle.
+// short ones).  Every solve runs on its worker's stream, so the GPU
+// interleaves the levels of up to `workers` problems; small problems, whose
+// levels are launch- and latency-bound, share the SMs instead of leaving
+// them idle.  A single solve runs each
+// checkpoint interval as one CUDA graph (a conditional WHILE node over the
+// level), but graphs launched on different streams were measured to run one
+// at a time (48 problems, 16 workers: 12.5 s with those graphs, 10.5-12.3 s
+// with plain graphs of 2-32 levels, 7.9 s with the level kernels launched
+// from the host), so a batch with more than one worker launches from the
+// host.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -80,7 +86,12 @@ std::vector<BatchOutcome> solve_amfls_batch(const std::vector<BatchItem>& items,
             o.worker = w;
             const auto ts = std::chrono::steady_clock::now();
             try {
-                o.result = solve_amfls(*items[i].op, items[i].b, items[i].options, items[i].x, s);
+                SolveOptions opts = items[i].options;
+                // CUDA graphs of different streams were measured to run
+                // their work one graph at a time: concurrent solves launch
+                // their level kernels from the host instead
+                if (workers > 1) opts.use_graphs = false;
+                o.result = solve_amfls(*items[i].op, items[i].b, opts, items[i].x, s);
                 o.ok = true;
             } catch (const std::exception& e) {
                 o.error = e.what();
