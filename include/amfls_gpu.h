@@ -348,7 +348,7 @@ int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, void* st
  * when it wins by at least 10% over the size / row-length rule's choice; the
  * row-vector kernel (rows binned by length, 1-32 lanes per row, no shared
  * memory) is timed as a third candidate and replaces the tiles when it beats
- * the kept tiling by 10%.
+ * the kept tiling by 5%.
  * chains[0], chains[1]: 0 when A's / the transpose's products use row
  * blocks, 1 chain groups, 2 the row-vector kernel; microseconds[0..3]: the
  * timed products of A with row blocks and with chain groups, then the
