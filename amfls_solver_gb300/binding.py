@@ -423,14 +423,16 @@ def solve_amfls_replay(op: DeviceOperator, b: torch.Tensor, replay, *,
                        regularization: float = 0.0, tolerance: float = 1e-8,
                        failure_probability: float = 1e-6, maximum_epochs: int = 0,
                        maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
-                       maximum_basis_size: int = 0, seed: int = 0, stream: int = 0):
+                       maximum_basis_size: int = 0, seed: int = 0, stream: int = 0,
+                       reduced_basis: bool = False):
     """AMFLS in schedule-replay mode: the width decisions at the controller's
     decision sites (amfls.cpp:323-354) take the candidate bits in `replay`
     (a sequence of 0/1) instead of the timing-driven cost gate's, so a
     widening solve recorded on the reference is reproduced whatever the
     timings.  Returns (SolveResult, decisions, overrun): the bit taken at
     every decision site and the number of sites beyond the list.  A test
-    mode; no counterpart in the reference's API."""
+    mode; no counterpart in the reference's API.  reduced_basis as in
+    solve_amfls."""
     if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
         raise ValueError("b must be a float64 CUDA vector of length rows on the operator's device")
     o = _native.default_options()
@@ -443,6 +445,7 @@ def solve_amfls_replay(op: DeviceOperator, b: torch.Tensor, replay, *,
     o.maximum_basis_size = int(maximum_basis_size)
     o.seed = _uint64(seed)
     o.stream = _uint64(stream)
+    o.reduced_basis = 1 if reduced_basis else 0
     rp = np.ascontiguousarray(np.asarray(list(replay), dtype=np.int32))
     cap = 1 << 16
     dec = np.zeros(cap, dtype=np.int32)

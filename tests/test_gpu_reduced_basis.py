@@ -133,3 +133,31 @@ def test_mixed_form_against_the_reference_on_a_tall_ridge_problem(amfls):
     print(f"\nmixed form vs reference: {r.depth} levels ({int(r.trace_float.shape[0])} cycles), "
           f"x relative difference {rel:.2e}, energy norm {hnorm(x - xr) / hnorm(xr):.2e}")
     assert rel <= 2 * tol * norm_m / np.sqrt(reg)
+
+
+def test_reduced_basis_through_a_widening_solve(amfls):
+    """A solve that widens (the reference's forced schedule on a 2000 x 500
+    ridge problem, replayed) starts at width one on the FP32 copy of the
+    basis and continues on the block path, which projects on the FP64 basis:
+    the replayed decisions, the reference's status and a certified result
+    with x within 2.5 tol of the reference's in the energy norm."""
+    import scipy.sparse as sp
+    from conftest import golden_options, load_replay
+
+    data, prob = load_replay("replay_csr_ridge_forced")
+    opts = golden_options(data)
+    reg, tol = opts["regularization"], opts["tolerance"]
+    op = amfls.DeviceOperator(_csr(prob))
+    r, decisions, overrun = amfls.solve_amfls_replay(
+        op, torch.from_numpy(prob.b).cuda(), [int(v) for v in data["replay"]], reduced_basis=True,
+        **opts)
+    assert overrun == 0
+    assert r.auxiliary_width > 0  # the solve widened
+    assert (r.status, r.stop_reason) == (int(data["status"]), int(data["stop_reason"]))
+    if r.status == 0:
+        assert r.relative_energy_error_upper_bound <= tol
+    a = sp.csr_matrix((prob.values, prob.column_indices, prob.row_offsets),
+                      shape=(prob.rows, prob.cols))
+    hnorm = lambda v: np.sqrt(np.linalg.norm(a @ v) ** 2 + reg * np.linalg.norm(v) ** 2)
+    x, xr = r.solution.cpu().numpy(), data["solution"]
+    assert hnorm(x - xr) <= 2.5 * tol * hnorm(xr)
