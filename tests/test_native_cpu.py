@@ -110,3 +110,44 @@ def test_callback_operator_needs_both_products(lib):
 def test_schedule_query_rejects_null_buffers(lib):
     rc = lib.amfls_gpu_csr_operator_schedule(None, None, None)
     assert rc == 1
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the C structs against the header itself: a C
+    program compiled from include/amfls_gpu.h prints every field's offset
+    and each struct's size."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"amfls_gpu_options": _native.Options, "amfls_gpu_result": _native.Result,
+               "amfls_gpu_baseline_options": _native.BaselineOptions,
+               "amfls_gpu_validation_error_model": _native.ValidationModel,
+               "amfls_gpu_operator_callbacks": _native.Callbacks}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "amfls_gpu.h"',
+             'int main(void) {']
+    for cname, mirror in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in mirror._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(HEADER.parent), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, mirror in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(mirror), cname
+        for field, _ in mirror._fields_:
+            assert got[(cname, field)] == getattr(mirror, field).offset, (cname, field)
+
+
+def test_reduced_basis_defaults_off_and_probe_checks_sizes(lib):
+    o = _native.default_options()
+    assert o.reduced_basis == 0 and o.use_graphs == 1
+    sec = (ctypes.c_double * 2)()
+    rc = lib.amfls_gpu_probe_reorthogonalization_reduced(0, 10, 1, None, sec, None)
+    assert rc == 1 and b"probe sizes must be positive" in lib.amfls_gpu_last_error()
