@@ -716,12 +716,14 @@ int reduced_sweep_grid() {
     int dev = 0;
     AMFLS_CUDA(cudaGetDevice(&dev));
     const int slot = dev >= 0 && dev < 64 ? dev : 0;
-    if (cached[slot] == 0) {
+    int g = __atomic_load_n(&cached[slot], __ATOMIC_RELAXED);
+    if (g == 0) {  // concurrent first callers compute the same value
         int a = 0;
         AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, vt_r32_kernel, kThreads, 0));
-        cached[slot] = std::max(1, a) * sm_count();
+        g = std::max(1, a) * sm_count();
+        __atomic_store_n(&cached[slot], g, __ATOMIC_RELAXED);
     }
-    return cached[slot];
+    return g;
 }
 
 // ----------------------------------------------------------------------------
