@@ -390,18 +390,29 @@ def _uint64(v: int) -> int:
     return int(v) & (2**64 - 1)
 
 
+def _reduced_storage(reduced_basis) -> int:
+    """reduced_basis argument -> options.reduced_basis: False / 0 off,
+    True / "fp32" / 1 an FP32 copy of the basis, "fp16" / 2 an FP16 copy."""
+    codes = {False: 0, None: 0, 0: 0, True: 1, 1: 1, "fp32": 1, 2: 2, "fp16": 2}
+    try:
+        return codes[reduced_basis]
+    except (KeyError, TypeError):
+        raise ValueError("reduced_basis must be False, True, 'fp32' or 'fp16'") from None
+
+
 def solve_amfls(op: DeviceOperator, b: torch.Tensor, *, regularization: float = 0.0,
                 tolerance: float = 1e-8, failure_probability: float = 1e-6,
                 maximum_epochs: int = 0, maximum_depth: int = 0,
                 maximum_auxiliary_width: int = 0, maximum_basis_size: int = 0, seed: int = 0,
-                stream: int = 0, reduced_basis: bool = False) -> SolveResult:
+                stream: int = 0, reduced_basis=False) -> SolveResult:
     """AMFLS on an existing DeviceOperator (CSR, dense, reduced or callback),
     the reference's C++ entry amfls::solve_amfls(op, b, options)
-    (include/amfls/amfls.hpp:22-25).  reduced_basis (not a reference option)
-    runs the first reorthogonalisation pass of width-one levels on an FP32
-    copy of the right basis, the sweeps of the mixed form's restart cycles;
-    a single solve of an ill-conditioned problem to FP64 accuracy can stall
-    with it (the certificate reports that)."""
+    (include/amfls/amfls.hpp:22-25).  reduced_basis (not a reference option:
+    True or "fp32", "fp16") runs the first reorthogonalisation pass of
+    width-one levels on an FP32 or FP16 copy of the right basis, the sweeps
+    of the mixed form's restart cycles; a single solve of an ill-conditioned
+    problem to FP64 accuracy can stall with it (the certificate reports
+    that)."""
     if b.device != op.device or b.dtype != torch.float64 or b.dim() != 1 or b.numel() != op.rows:
         raise ValueError("b must be a float64 CUDA vector of length rows on the operator's device")
     o = _native.default_options()
@@ -414,7 +425,7 @@ def solve_amfls(op: DeviceOperator, b: torch.Tensor, *, regularization: float = 
     o.maximum_basis_size = int(maximum_basis_size)
     o.seed = _uint64(seed)
     o.stream = _uint64(stream)
-    o.reduced_basis = 1 if reduced_basis else 0
+    o.reduced_basis = _reduced_storage(reduced_basis)
     native = []
     return _with_extras(_decode(_solve_raw("amfls", op, b, o, native)), native[0])
 
@@ -424,7 +435,7 @@ def solve_amfls_replay(op: DeviceOperator, b: torch.Tensor, replay, *,
                        failure_probability: float = 1e-6, maximum_epochs: int = 0,
                        maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
                        maximum_basis_size: int = 0, seed: int = 0, stream: int = 0,
-                       reduced_basis: bool = False):
+                       reduced_basis=False):
     """AMFLS in schedule-replay mode: the width decisions at the controller's
     decision sites (amfls.cpp:323-354) take the candidate bits in `replay`
     (a sequence of 0/1) instead of the timing-driven cost gate's, so a
@@ -445,7 +456,7 @@ def solve_amfls_replay(op: DeviceOperator, b: torch.Tensor, replay, *,
     o.maximum_basis_size = int(maximum_basis_size)
     o.seed = _uint64(seed)
     o.stream = _uint64(stream)
-    o.reduced_basis = 1 if reduced_basis else 0
+    o.reduced_basis = _reduced_storage(reduced_basis)
     rp = np.ascontiguousarray(np.asarray(list(replay), dtype=np.int32))
     cap = 1 << 16
     dec = np.zeros(cap, dtype=np.int32)
@@ -531,12 +542,13 @@ def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
                     maximum_depth: int = 0, maximum_auxiliary_width: int = 0,
                     maximum_basis_size: int = 0, seed: int = 0, stream: int = 0,
                     reduced: "DeviceOperator | None" = None,
-                    reduced_basis: bool = False) -> SolveResult:
+                    reduced_basis=False) -> SolveResult:
     """Mixed-precision AMFLS: inner solves refined in FP64; the certified
     FP64 validation on the original matrix decides termination.  `values`
     is the inner products' precision ("fp32", "bf16", or "fp64" for inner
-    solves on the FP64 operator itself); `reduced_basis` runs the inner
-    solves' first reorthogonalisation pass on an FP32 copy of the basis.
+    solves on the FP64 operator itself); `reduced_basis` (True or "fp32",
+    "fp16") runs the inner solves' first reorthogonalisation pass on an FP32
+    or FP16 copy of the basis.
     With maximum_depth set and a tiny inner_tolerance every inner solve is
     one restart cycle of maximum_depth levels.  `matrix` is a CUDA tensor or
     a DeviceOperator; `reduced` reuses an existing reduced operator.  Work
@@ -560,7 +572,7 @@ def run_amfls_mixed(matrix, b: torch.Tensor, *, values: str = "fp32",
     o.maximum_basis_size = int(maximum_basis_size)
     o.seed = _uint64(seed)
     o.stream = _uint64(stream)
-    o.reduced_basis = 1 if reduced_basis else 0
+    o.reduced_basis = _reduced_storage(reduced_basis)
     b = b.contiguous()
     x = torch.empty(op.cols, dtype=torch.float64, device=b.device)
     res = _native.Result()

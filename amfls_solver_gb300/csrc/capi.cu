@@ -79,7 +79,7 @@ amfls_gpu::SolveOptions to_options(const amfls_gpu_options* o) {
     s.stop_early = o->stop_early != 0;
     s.time_operators = o->time_operators != 0;
     s.use_graphs = o->use_graphs != 0;
-    s.reduced_basis = o->reduced_basis != 0;
+    s.reduced_basis = o->reduced_basis;
     return s;
 }
 
@@ -486,12 +486,13 @@ int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream,
     });
 }
 
-int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, void* stream,
-                                                double* seconds, double* max_rel_error) {
+int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, int storage,
+                                                void* stream, double* seconds,
+                                                double* max_rel_error) {
     return guarded([&] {
         if (seconds == nullptr) throw std::invalid_argument("seconds must not be null");
-        amfls_gpu::probe_reorthogonalization_reduced(n, k, reps, as_stream(stream), seconds,
-                                                     max_rel_error);
+        amfls_gpu::probe_reorthogonalization_reduced(n, k, reps, storage, as_stream(stream),
+                                                     seconds, max_rel_error);
     });
 }
 

@@ -33,12 +33,13 @@ struct SolveOptions {
     // latest least-squares iterate has the smallest error in the normal
     // equations' energy norm while the backward error need not be monotone.
     bool latest_at_limit = false;
-    // Width-one levels keep an FP32 copy of the right basis and run their
-    // first reorthogonalisation pass on it, redoing it in FP64 when the
-    // coefficients are not small (see the reduced-basis sweeps in
-    // workspace.cu).  Not part of the reference's options: the
-    // mixed-precision form's reduced sweeps.
-    bool reduced_basis = false;
+    // 1 (FP32) or 2 (FP16): width-one levels keep a reduced copy of the
+    // right basis and run their first reorthogonalisation pass on it,
+    // redoing it in FP64 when the coefficients are not small (see the
+    // reduced-basis sweeps in workspace.cu); 0 keeps every sweep FP64.  Not
+    // part of the reference's options: the mixed-precision form's reduced
+    // sweeps.
+    int reduced_basis = 0;
 };
 
 // RunStatistics (include/amfls/least_squares_result.hpp:57-109).

@@ -30,6 +30,8 @@
 #include <stdexcept>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 #include "vector_ops.hpp"
 #include "workspace.hpp"
@@ -470,6 +472,38 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
 // failure; it never certifies a wrong x).
 constexpr double kReducedCoeffBound = 1e-3;
 
+// Storage of the basis copy: FP32, or FP16 holding 2^8 v (the entries of a
+// unit vector then stay in FP16's normal range down to 2.4e-7; products and
+// sums run in FP32 and the results are scaled back by 2^-8, exactly).
+template <typename S>
+struct RedStore;
+template <>
+struct RedStore<float> {
+    static constexpr float kInvScale = 1.0f;
+    __device__ static void load8(const float* p, float v[8]) {
+        const float4 a = __ldcs(reinterpret_cast<const float4*>(p));
+        const float4 b = __ldcs(reinterpret_cast<const float4*>(p) + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    }
+    __device__ static float store(double v) { return __double2float_rn(v); }
+};
+template <>
+struct RedStore<__half> {
+    static constexpr float kInvScale = 1.0f / 256.0f;
+    __device__ static void load8(const __half* p, float v[8]) {
+        const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
+        const __half2* h = reinterpret_cast<const __half2*>(&u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 f = __half22float2(h[i]);
+            v[2 * i] = f.x;
+            v[2 * i + 1] = f.y;
+        }
+    }
+    __device__ static __half store(double v) { return __float2half_rn(__double2float_rn(v * 256.0)); }
+};
+
 // r~ = fl32(r) for the reduced pass (only when the level projects).
 __global__ void round_residual_kernel(const double* __restrict__ r, float* __restrict__ r32, int n,
                                       const DevState* st) {
@@ -498,8 +532,9 @@ inline long long reduced_part_doubles(int grid, long long panels) {
 // finishes the last panel adds the panels' sums of c^2 in panel order and
 // decides whether the level redoes the pass in FP64.  Deterministic for a
 // fixed grid.
+template <typename S>
 __global__ void __launch_bounds__(kThreads)
-vt_r32_kernel(const float* const* __restrict__ panels, int n, const float* __restrict__ r,
+vt_r32_kernel(const S* const* __restrict__ panels, int n, const float* __restrict__ r,
               double* __restrict__ c, float* __restrict__ c32, double* part, double* panel_sq,
               unsigned* panel_tickets, unsigned* all_ticket, DevState* st) {
     if (!st->go) return;
@@ -514,7 +549,7 @@ vt_r32_kernel(const float* const* __restrict__ panels, int n, const float* __res
     __shared__ int last;
     for (int t = blockIdx.x; t < P * chunks; t += gridDim.x) {
         const int p = t / chunks, chunk = t - p * chunks;
-        const float* __restrict__ vp = panels[p];
+        const S* __restrict__ vp = panels[p];
         const long long row0 = (long long)chunk * chunk_rows;
         const long long row1 = min((long long)n, row0 + chunk_rows);
         double acc[8];
@@ -527,32 +562,24 @@ vt_r32_kernel(const float* const* __restrict__ panels, int n, const float* __res
 #pragma unroll
             for (int i = 0; i < 8; ++i) s8[i] = 0.f;
             for (int step = 0; step < 4 && base < row1; ++step, base += 256) {
-                float4 a[4][2];
+                float a[4][8];
                 float rv[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const long long row = base + j * 8 + rsub;
                     if (row < row1) {
-                        const float4* src = reinterpret_cast<const float4*>(vp + row * 32 + q * 8);
-                        a[j][0] = __ldcs(src);
-                        a[j][1] = __ldcs(src + 1);
+                        RedStore<S>::load8(vp + row * 32 + q * 8, a[j]);
                         rv[j] = __ldg(r + row);
                     } else {
-                        a[j][0] = make_float4(0.f, 0.f, 0.f, 0.f);
-                        a[j][1] = a[j][0];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) a[j][i] = 0.f;
                         rv[j] = 0.f;
                     }
                 }
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    s8[0] = fmaf(a[j][0].x, rv[j], s8[0]);
-                    s8[1] = fmaf(a[j][0].y, rv[j], s8[1]);
-                    s8[2] = fmaf(a[j][0].z, rv[j], s8[2]);
-                    s8[3] = fmaf(a[j][0].w, rv[j], s8[3]);
-                    s8[4] = fmaf(a[j][1].x, rv[j], s8[4]);
-                    s8[5] = fmaf(a[j][1].y, rv[j], s8[5]);
-                    s8[6] = fmaf(a[j][1].z, rv[j], s8[6]);
-                    s8[7] = fmaf(a[j][1].w, rv[j], s8[7]);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) s8[i] = fmaf(a[j][i], rv[j], s8[i]);
                 }
             }
 #pragma unroll
@@ -588,6 +615,7 @@ vt_r32_kernel(const float* const* __restrict__ panels, int n, const float* __res
             double v = 0.0;
             for (int ch = 0; ch < chunks; ++ch)
                 v += __ldcg(&part[((long long)p * chunks + ch) * 32 + threadIdx.x]);
+            v *= (double)RedStore<S>::kInvScale;  // exact: a power of two
             const int col = p * 32 + threadIdx.x;
             double sq = 0.0;
             if (col < k) {
@@ -621,8 +649,9 @@ vt_r32_kernel(const float* const* __restrict__ panels, int n, const float* __res
 // r <- r - fl64(V~ c~) with ||r||^2 and the DGKS decision of the first pass
 // (as v_c_kernel's kHookRightPass1); 32 rows per block, warps split the
 // panels.  Skipped when the level redoes the pass in FP64.
+template <typename S>
 __global__ void __launch_bounds__(kThreads)
-v_c32_kernel(const float* const* __restrict__ panels, int n, const float* __restrict__ c,
+v_c32_kernel(const S* const* __restrict__ panels, int n, const float* __restrict__ c,
              double* r, double* partials, unsigned* ticket, DevState* st, int m_rows) {
     if (!st->go || st->k == 0 || st->sweep_fp64) return;
     const int k = st->k;
@@ -633,44 +662,36 @@ v_c32_kernel(const float* const* __restrict__ panels, int n, const float* __rest
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 2
     for (int p = warp; p < P; p += 8) {
-        const float* __restrict__ vp = panels[p];
+        const S* __restrict__ vp = panels[p];
         float cv[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int col = p * 32 + q * 8 + i;
             cv[i] = col < k ? c[col] : 0.f;
         }
-        float4 a[4][2];
+        float a[4][8];
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
             const long long row = row0 + s * 8 + rsub;
             if (row < n) {
-                const float4* src = reinterpret_cast<const float4*>(vp + row * 32 + q * 8);
-                a[s][0] = __ldcs(src);
-                a[s][1] = __ldcs(src + 1);
+                RedStore<S>::load8(vp + row * 32 + q * 8, a[s]);
             } else {
-                a[s][0] = make_float4(0.f, 0.f, 0.f, 0.f);
-                a[s][1] = a[s][0];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) a[s][i] = 0.f;
             }
         }
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
             float t = acc[s];
-            t = fmaf(a[s][0].x, cv[0], t);
-            t = fmaf(a[s][0].y, cv[1], t);
-            t = fmaf(a[s][0].z, cv[2], t);
-            t = fmaf(a[s][0].w, cv[3], t);
-            t = fmaf(a[s][1].x, cv[4], t);
-            t = fmaf(a[s][1].y, cv[5], t);
-            t = fmaf(a[s][1].z, cv[6], t);
-            t = fmaf(a[s][1].w, cv[7], t);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) t = fmaf(a[s][i], cv[i], t);
             acc[s] = t;
         }
     }
     double accd[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        accd[s] = (double)acc[s];
+        accd[s] = (double)acc[s] * (double)RedStore<S>::kInvScale;
         accd[s] += __shfl_xor_sync(0xffffffffu, accd[s], 1);
         accd[s] += __shfl_xor_sync(0xffffffffu, accd[s], 2);
     }
@@ -719,7 +740,12 @@ int reduced_sweep_grid() {
     int g = __atomic_load_n(&cached[slot], __ATOMIC_RELAXED);
     if (g == 0) {  // concurrent first callers compute the same value
         int a = 0;
-        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, vt_r32_kernel, kThreads, 0));
+        int b = 0;
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, vt_r32_kernel<float>,
+                                                                 kThreads, 0));
+        AMFLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, vt_r32_kernel<__half>,
+                                                                 kThreads, 0));
+        a = std::min(a, b);
         g = std::max(1, a) * sm_count();
         __atomic_store_n(&cached[slot], g, __ATOMIC_RELAXED);
     }
@@ -974,21 +1000,22 @@ long long sweep_part_doubles(int n, long long panels, int grid) {
 
 // v = r / ||r|| into V's new column (and the FP32 copy's, when kept) and a
 // contiguous copy.
+template <typename S = float>
 __global__ void normalize_right_kernel(const double* r, int n, double* const* panels,
                                        double* vnew, DevState* st,
-                                       float* const* panels32 = nullptr) {
+                                       S* const* shadow = nullptr) {
     if (!st->go || !st->right_rank) return;
     const double inv = st->inv_right;
     const int k = st->k;
     double* vcol = panels[k >> 5] + (k & 31);
-    float* vcol32 = panels32 ? panels32[k >> 5] + (k & 31) : nullptr;
+    S* vcol_s = shadow ? shadow[k >> 5] + (k & 31) : nullptr;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->t_mark = global_ns();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const double v = r[i] * inv;
         vcol[i * 32] = v;
         vnew[i] = v;
-        if (vcol32) vcol32[i * 32] = __double2float_rn(v);
+        if (vcol_s) vcol_s[i * 32] = RedStore<S>::store(v);
     }
 }
 
@@ -1196,12 +1223,13 @@ void PanelStoreT<T>::ensure_columns(int cols) {
 
 template class PanelStoreT<double>;
 template class PanelStoreT<float>;
+template class PanelStoreT<__half>;
 
 // --------------------------------------------------------- workspace ----
 
 Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regularization,
                      int maximum_basis_size, cudaStream_t stream, bool time_operators,
-                     bool use_graphs, bool reduced_basis)
+                     bool use_graphs, int reduced_basis)
     : op_(op), stream_(stream), m_(op.rows()), n_(op.cols()), reg_(regularization),
       time_ops_(time_operators), use_graphs_(use_graphs), b_(d_b) {
     if (m_ <= 0 || n_ <= 0) throw std::invalid_argument("block Golub-Kahan operator dimensions must be positive");
@@ -1240,10 +1268,19 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     stream_alloc(&U_, sizeof(double) * m_ * ucap_, stream_);
     V_ = std::make_unique<PanelStore>(n_, static_cast<int>(max_panels), stream_);
     V_->ensure_columns(1);  // panel 0 exists (zeroed) before any level runs
-    reduced_basis_ = reduced_basis;
+    if (reduced_basis != kReducedOff && reduced_basis != kReducedFp32 &&
+        reduced_basis != kReducedFp16)
+        throw std::invalid_argument("reduced_basis must be 0 (off), 1 (FP32) or 2 (FP16)");
+    reduced_storage_ = reduced_basis;
+    reduced_basis_ = reduced_basis != kReducedOff;
     if (reduced_basis_) {
-        V32_ = std::make_unique<PanelStore32>(n_, static_cast<int>(max_panels), stream_);
-        V32_->ensure_columns(1);
+        if (reduced_storage_ == kReducedFp16) {
+            V16_ = std::make_unique<PanelStore16>(n_, static_cast<int>(max_panels), stream_);
+            V16_->ensure_columns(1);
+        } else {
+            V32_ = std::make_unique<PanelStore32>(n_, static_cast<int>(max_panels), stream_);
+            V32_->ensure_columns(1);
+        }
         red_grid_ = reduced_sweep_grid();
         stream_alloc(&r32_, sizeof(float) * n_, stream_);
         stream_alloc(&panel_sq_, sizeof(double) * max_panels, stream_);
@@ -1433,17 +1470,27 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
         round_residual_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0,
                                 s>>>(R_, r32_, n_, dstate_);
         AMFLS_LAUNCHED();
-        vt_r32_kernel<<<red_grid_, kThreads, 0, s>>>(V32_->device_table(), n_, r32_, c1_, c32_,
-                                                     red_part_, panel_sq_, red_tickets_,
-                                                     red_tickets_ + sweep_panels_, dstate_);
+        if (V16_)
+            vt_r32_kernel<__half><<<red_grid_, kThreads, 0, s>>>(
+                V16_->device_table(), n_, r32_, c1_, c32_, red_part_, panel_sq_, red_tickets_,
+                red_tickets_ + sweep_panels_, dstate_);
+        else
+            vt_r32_kernel<float><<<red_grid_, kThreads, 0, s>>>(
+                V32_->device_table(), n_, r32_, c1_, c32_, red_part_, panel_sq_, red_tickets_,
+                red_tickets_ + sweep_panels_, dstate_);
         AMFLS_LAUNCHED();
         vt_r_kernel<<<dim3(pcap, chunks), kThreads, 0, s>>>(V_->device_table(), n_, chunk_rows,
                                                             R_, c1_, partials_, counter_ + 64,
                                                             dstate_, 1, 1);
         AMFLS_LAUNCHED();
-        v_c32_kernel<<<(int)tiles, kThreads, 0, s>>>(V32_->device_table(), n_, c32_, R_,
-                                                     partials_ + vc_partials_offset_, counter_ + 3,
-                                                     dstate_, m_);
+        if (V16_)
+            v_c32_kernel<__half><<<(int)tiles, kThreads, 0, s>>>(
+                V16_->device_table(), n_, c32_, R_, partials_ + vc_partials_offset_, counter_ + 3,
+                dstate_, m_);
+        else
+            v_c32_kernel<float><<<(int)tiles, kThreads, 0, s>>>(
+                V32_->device_table(), n_, c32_, R_, partials_ + vc_partials_offset_, counter_ + 3,
+                dstate_, m_);
         AMFLS_LAUNCHED();
         v_c_kernel<<<rare_grid, kThreads, 0, s>>>(
             V_->device_table(), n_, -1, c1_, R_, R_, 1, partials_ + vc_partials_offset_,
@@ -1474,8 +1521,13 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
             AMFLS_LAUNCHED();
         }
     }
-    normalize_right_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0, s>>>(
-        R_, n_, V_->device_table(), vnew_, dstate_, reduced ? V32_->device_table() : nullptr);
+    const int ngrid = (int)std::min<long long>(grid_cap(), (n_ + 255) / 256);
+    if (reduced && V16_)
+        normalize_right_kernel<__half><<<ngrid, 256, 0, s>>>(R_, n_, V_->device_table(), vnew_,
+                                                            dstate_, V16_->device_table());
+    else
+        normalize_right_kernel<float><<<ngrid, 256, 0, s>>>(
+            R_, n_, V_->device_table(), vnew_, dstate_, reduced ? V32_->device_table() : nullptr);
     AMFLS_LAUNCHED();
     // y = A v - ||r|| u, with ||A v||, ||y||, u.y
     Epilogue el;
@@ -1554,6 +1606,7 @@ void Workspace::advance_to(int target_depth) {
     ensure_t_capacity(host_.k + levels + 2);
     V_->ensure_columns(host_.k + levels + 1);
     if (V32_) V32_->ensure_columns(host_.k + levels + 1);
+    if (V16_) V16_->ensure_columns(host_.k + levels + 1);
     const int pneed = (host_.k + levels + 31) / 32;
     int pcap = 4;
     while (pcap < pneed) pcap *= 2;
@@ -1641,7 +1694,8 @@ __global__ void probe_fill_kernel(double* const* panels, int n, int k, double* r
     }
 }
 
-__global__ void probe_round_kernel(double* const* panels, float* const* panels32, int n, int k,
+template <typename S>
+__global__ void probe_round_kernel(double* const* panels, S* const* shadow, int n, int k,
                                    const double* r, float* r32) {
     const long long total = (long long)n * 32;
     const int P = (k + 31) / 32;
@@ -1649,19 +1703,17 @@ __global__ void probe_round_kernel(double* const* panels, float* const* panels32
          i += (long long)gridDim.x * blockDim.x) {
         const int p = (int)(i / total);
         const long long e = i - (long long)p * total;
-        panels32[p][e] = __double2float_rn(panels[p][e]);
+        shadow[p][e] = RedStore<S>::store(panels[p][e]);
         if (p == 0 && e % 32 == 0) r32[e / 32] = __double2float_rn(r[e / 32]);
     }
 }
 
-}  // namespace
-
-void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, double seconds[2],
-                                       double* max_rel_error) {
-    if (n <= 0 || k <= 0 || reps <= 0) throw std::invalid_argument("probe sizes must be positive");
+template <typename S>
+void probe_reduced(int n, int k, int reps, cudaStream_t s, double seconds[2],
+                   double* max_rel_error) {
     const int P = (k + 31) / 32;
     PanelStore V(n, P, s);
-    PanelStore32 V32(n, P, s);
+    PanelStoreT<S> V32(n, P, s);
     V.ensure_columns(k);
     V32.ensure_columns(k);
     const int grid = reduced_sweep_grid();
@@ -1700,8 +1752,8 @@ void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, d
     AMFLS_CUDA(cudaMemcpyAsync(st, &h, sizeof(DevState), cudaMemcpyHostToDevice, s));
     probe_fill_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), n, k, r);
     AMFLS_LAUNCHED();
-    probe_round_kernel<<<grid_cap(), 256, 0, s>>>(V.device_table(), V32.device_table(), n, k, r,
-                                                  r32);
+    probe_round_kernel<S><<<grid_cap(), 256, 0, s>>>(V.device_table(), V32.device_table(), n, k,
+                                                     r, r32);
     AMFLS_LAUNCHED();
     // the FP64 projection of the same basis, for the error
     {
@@ -1711,15 +1763,15 @@ void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, d
         AMFLS_LAUNCHED();
     }
     auto vt = [&] {
-        vt_r32_kernel<<<grid, kThreads, 0, s>>>(V32.device_table(), n, r32, c, c32, part, psq,
-                                                tickets, tickets + 2 * P + 1, st);
+        vt_r32_kernel<S><<<grid, kThreads, 0, s>>>(V32.device_table(), n, r32, c, c32, part, psq,
+                                                   tickets, tickets + 2 * P + 1, st);
         AMFLS_LAUNCHED();
     };
     // r is restored by the caller's pattern only once; the subtraction of
     // the tiny probe coefficients leaves it finite, which is all timing needs
     auto vc = [&] {
-        v_c32_kernel<<<(int)tiles, kThreads, 0, s>>>(V32.device_table(), n, c32, r, vcpart,
-                                                     tickets + P, st, n);
+        v_c32_kernel<S><<<(int)tiles, kThreads, 0, s>>>(V32.device_table(), n, c32, r, vcpart,
+                                                        tickets + P, st, n);
         AMFLS_LAUNCHED();
     };
     vt();
@@ -1762,6 +1814,19 @@ void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t s, d
     stream_free(tickets, s);
     stream_free(st, s);
     stream_wait(s);
+}
+
+}  // namespace
+
+void probe_reorthogonalization_reduced(int n, int k, int reps, int storage, cudaStream_t s,
+                                       double seconds[2], double* max_rel_error) {
+    if (n <= 0 || k <= 0 || reps <= 0) throw std::invalid_argument("probe sizes must be positive");
+    if (storage == kReducedFp16)
+        probe_reduced<__half>(n, k, reps, s, seconds, max_rel_error);
+    else if (storage == kReducedFp32)
+        probe_reduced<float>(n, k, reps, s, seconds, max_rel_error);
+    else
+        throw std::invalid_argument("probe storage must be 1 (FP32) or 2 (FP16)");
 }
 
 void probe_reorthogonalization(int n, int k, int reps, cudaStream_t s, double seconds[2]) {

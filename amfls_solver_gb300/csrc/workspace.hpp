@@ -17,6 +17,7 @@
 // block path.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <memory>
@@ -52,14 +53,19 @@ private:
 };
 using PanelStore = PanelStoreT<double>;
 using PanelStore32 = PanelStoreT<float>;
+using PanelStore16 = PanelStoreT<__half>;
+
+// Storage of the reduced-basis copy of V (options.reduced_basis).
+enum ReducedStorage { kReducedOff = 0, kReducedFp32 = 1, kReducedFp16 = 2 };
 
 class Workspace {
 public:
-    // reduced_basis: width-one levels keep an FP32 copy of V and run their
-    // first projection pass on it (see enqueue_level_kernels).
+    // reduced_basis (a ReducedStorage): width-one levels keep an FP32 or FP16
+    // copy of V and run their first projection pass on it (see
+    // enqueue_level_kernels).
     Workspace(const DeviceOperator& op, const double* d_b, double regularization,
               int maximum_basis_size, cudaStream_t stream, bool time_operators,
-              bool use_graphs = true, bool reduced_basis = false);
+              bool use_graphs = true, int reduced_basis = kReducedOff);
     ~Workspace();
     Workspace(const Workspace&) = delete;
     Workspace& operator=(const Workspace&) = delete;
@@ -106,7 +112,7 @@ public:
 
     // true once a level or seed wider than one column has been seen
     bool block_mode() const { return block_mode_; }
-    // whether width-one levels project on the FP32 copy of V
+    // whether width-one levels project on a reduced copy of V
     bool reduced_basis() const { return reduced_basis_; }
 
 private:
@@ -176,7 +182,9 @@ private:
     // reduced-basis sweeps: FP32 copy of V, r rounded to FP32, the FP32
     // coefficients, per-panel sums of c^2 and the tickets (panels | all)
     bool reduced_basis_ = false;
+    int reduced_storage_ = kReducedOff;
     std::unique_ptr<PanelStore32> V32_;
+    std::unique_ptr<PanelStore16> V16_;
     float* r32_ = nullptr;
     float* c32_ = nullptr;
     double* panel_sq_ = nullptr;
@@ -265,11 +273,13 @@ private:
 // panel layout filled with a fixed pattern: `reps` launches of each, CUDA
 // events on `stream`; seconds[0] / seconds[1] receive the mean per launch.
 void probe_reorthogonalization(int n, int k, int reps, cudaStream_t stream, double seconds[2]);
-// The same for the reduced-basis sweeps (FP32 copy of V, FP32 products,
-// FP64 subtraction): seconds[0] / seconds[1] the V~^T r and r - V~ c passes;
+// The same for the reduced-basis sweeps (an FP32 or FP16 copy of V, a
+// ReducedStorage; FP32 products, FP64 subtraction): seconds[0] / seconds[1]
+// the V~^T r and r - V~ c passes;
 // max_rel_error[0] receives max |c - c_fp64| / ||r|| over the columns (the
 // projection's error against the FP64 sweep on the same basis).
-void probe_reorthogonalization_reduced(int n, int k, int reps, cudaStream_t stream,
-                                       double seconds[2], double* max_rel_error);
+void probe_reorthogonalization_reduced(int n, int k, int reps, int storage,
+                                       cudaStream_t stream, double seconds[2],
+                                       double* max_rel_error);
 
 }  // namespace amfls_gpu

@@ -68,6 +68,8 @@ METRIC = ("time-to-tol (s) mixed+batched+learned vs plain FP64 AMFLS on GB300; "
           "SpMM HBM GB/s")
 SEED = 20251203
 C3_CYCLE = 2000  # restart-cycle length of the chosen form on the 2M x 500k problem
+C3_STORAGE = "fp16"  # precision of the chosen form's copy of the basis ("fp32" or "fp16")
+C3_STORAGE_CODE = {"fp32": 1, "fp16": 2}[C3_STORAGE]
 # DRAM bytes of one V^T r + r - V c pair measured by ncu (--set full) on the
 # warp-task sweeps at n = 5000, k = 1900: 76.875 + 1.307 MB and 76.860 + 1.436 MB
 SWEEP_CAPTURE = {"n": 5000, "k": 1900, "bytes": (76.875 + 1.307 + 76.860 + 1.436) * 1e6}
@@ -247,21 +249,23 @@ def reorth_roofline(lib, n, k, stream, peak, peak_kind):
             "algorithmic_bytes": {"vt_r": bytes_vt, "v_c": bytes_vc}}
 
 
-def reduced_reorth_roofline(lib, n, k, stream, peak, peak_kind):
-    """The reduced-basis sweeps (FP32 copy of V: c = V~^T r~, r -= fl64(V~ c~))
-    timed live on `stream` at basis size k
+def reduced_reorth_roofline(lib, n, k, stream, peak, peak_kind, storage):
+    """The reduced-basis sweeps (an FP32 (storage 1) or FP16 (2) copy of V:
+    c = V~^T r~, r -= fl64(V~ c~)) timed live on `stream` at basis size k
     (amfls_gpu_probe_reorthogonalization_reduced)."""
     import ctypes
     from amfls_solver_gb300 import _native
     secs = (ctypes.c_double * 2)()
     err = ctypes.c_double()
     _native.check(lib.amfls_gpu_probe_reorthogonalization_reduced(
-        n, k, 50, ctypes.c_void_p(stream), secs, ctypes.byref(err)))
+        n, k, 50, storage, ctypes.c_void_p(stream), secs, ctypes.byref(err)))
     vt, vc = secs[0], secs[1]
-    bytes_vt = 4.0 * n * k + 4.0 * n * ((k + 31) // 32)  # V~ once, r~ once per panel
-    bytes_vc = 4.0 * n * k + 16.0 * n                    # V~ once, r in and out
+    e = 4.0 if storage == 1 else 2.0                    # bytes per element of V~
+    bytes_vt = e * n * k + 4.0 * n * ((k + 31) // 32)  # V~ once, r~ once per panel
+    bytes_vc = e * n * k + 16.0 * n                    # V~ once, r in and out
     achieved = (bytes_vt + bytes_vc) / (vt + vc) / 1e9
-    return {"kernel": "vt_r32_kernel (c = V~^T r~) + v_c32_kernel (r -= fl64(V~ c~))",
+    return {"kernel": ("vt_r32_kernel (c = V~^T r~) + v_c32_kernel (r -= fl64(V~ c~)), "
+                       f"{'FP32' if storage == 1 else 'FP16'} copy of V"),
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
             "basis_rows": n, "basis_cols": k, "launch_us": {"vt_r32": vt * 1e6, "v_c32": vc * 1e6},
@@ -364,13 +368,13 @@ def c3_measurement(dev):
         # C3_CYCLE levels whose first reorthogonalisation pass runs on an FP32
         # copy of the basis (products, recurrence and validation in FP64)
         mixed, t_mixed = timed_solve(lambda: amfls.run_amfls_mixed(
-            op, b, values="fp64", reduced_basis=True, inner_tolerance=1e-14,
+            op, b, values="fp64", reduced_basis=C3_STORAGE, inner_tolerance=1e-14,
             maximum_refinements=40, maximum_depth=C3_CYCLE, **opts))
         d = describe(mixed, t_mixed)
         xm = mixed.solution
         d.update({"form": (f"FP64 residual correction, restart cycles of {C3_CYCLE} levels, "
-                           "reduced-basis sweeps (FP32 copy of V, FP64 subtraction), FP64 "
-                           "operator products"),
+                           f"reduced-basis sweeps ({C3_STORAGE.upper()} copy of V, FP64 "
+                           "subtraction), FP64 operator products"),
                   "cycles": int(mixed.trace_float.shape[0]),
                   "cycle_certificates": [float(v) for v in mixed.trace_float[:, 17]],
                   "reduced_basis_levels": mixed.reduced_basis_levels,
@@ -692,7 +696,8 @@ def run_ours(args, world, rank, local):
                                                  stream.cuda_stream, peak, peak_kind)
             if "mixed" in c3:
                 c3["mixed"]["roofline"] = reduced_reorth_roofline(
-                    lib, c3["cols"], C3_CYCLE // 2, stream.cuda_stream, peak, peak_kind)
+                    lib, c3["cols"], C3_CYCLE // 2, stream.cuda_stream, peak, peak_kind,
+                    C3_STORAGE_CODE)
                 c3["mixed"]["roofline"]["note"] = "at the mean basis size of a restart cycle"
             legs["c3"] = c3
     if rank != 0:

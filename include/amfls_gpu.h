@@ -79,17 +79,19 @@ typedef struct {
                                     interval (default 1); 0 launches the same kernels one by
                                     one, e.g. for per-kernel profiling */
     int reduced_basis;           /* mixed-precision sweeps (default 0; no counterpart in the
-                                    reference): width-one levels keep an FP32 copy of the
-                                    right basis V and run their first reorthogonalisation
-                                    pass on it (FP32 products, FP64 subtraction), redoing it
-                                    in FP64 when its coefficients exceed 1e-3 ||r||; the
+                                    reference): 1 (FP32) or 2 (FP16, holding 2^8 v):
+                                    width-one levels keep a reduced copy of the right basis V
+                                    and run their first reorthogonalisation pass on it (FP32
+                                    products, FP64 subtraction), redoing it in FP64 when its
+                                    coefficients exceed 1e-3 ||r||; the
                                     recurrence, products, DGKS second pass, projected solve
                                     and validation stay FP64.  V then stays orthogonal to
                                     about FP32 rounding / sqrt(rows), which suits the restart
                                     cycles of amfls_gpu_solve_amfls_mixed; a single solve of
                                     an ill-conditioned problem to FP64 accuracy can stall on
                                     it (reported by the certificate, never a false success).
-                                    Costs 4 extra bytes per basis element of device memory. */
+                                    Costs 4 (FP32) or 2 (FP16) extra bytes per basis element
+                                    of device memory. */
 } amfls_gpu_options;
 
 /* LeastSquaresResult, packed like the torch binding's tensors. */
@@ -332,13 +334,15 @@ int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b
 int amfls_gpu_probe_reorthogonalization(int n, int k, int reps, void* stream, double* seconds);
 
 /* The same for the reduced-basis sweeps (options.reduced_basis; no
- * counterpart in the reference): the first pass c = V~^T r~ on the FP32 copy
- * of the basis and r -> r - fl64(V~ c~).  seconds[0] / seconds[1] as above;
- * *max_rel_error (may be NULL) receives max_j |c_j - c64_j| / ||r||, the
- * projection's deviation from the FP64 sweep on the same basis.  Allocates
- * 12 n k bytes for the duration of the call; synchronous. */
-int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, void* stream,
-                                                double* seconds, double* max_rel_error);
+ * counterpart in the reference): the first pass c = V~^T r~ on the FP32
+ * (storage 1) or FP16 (storage 2) copy of the basis and r -> r - fl64(V~ c~).
+ * seconds[0] / seconds[1] as above; *max_rel_error (may be NULL) receives
+ * max_j |c_j - c64_j| / ||r||, the projection's deviation from the FP64
+ * sweep on the same basis.  Allocates up to 12 n k bytes for the duration of
+ * the call; synchronous. */
+int amfls_gpu_probe_reorthogonalization_reduced(int n, int k, int reps, int storage,
+                                                void* stream, double* seconds,
+                                                double* max_rel_error);
 
 /* The tiling of a CSR operator's single-column products (no counterpart in
  * the reference, whose products are scalar loops; sparse_csr_operator.cpp:

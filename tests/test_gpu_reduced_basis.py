@@ -1,18 +1,19 @@
 """GPU tests of the reduced-basis sweeps (options.reduced_basis; no
 counterpart in the reference, whose sweeps are FP64 BLAS calls).
 
-Width-one levels keep an FP32 copy of the right basis V and run their first
-reorthogonalisation pass on it: c = V~^T fl32(r) with FP32 products summed in
-FP32 over runs of 16 rows per lane and in FP64 above that, then
-r <- r - fl64(V~ fl32(c)).  The recurrence, the operator products, the DGKS
+Width-one levels keep an FP32 or FP16 copy (FP16 holding 2^8 v) of the
+right basis V and run their first reorthogonalisation pass on it:
+c = V~^T fl32(r) with FP32 products summed in FP32 over runs of 16 rows per
+lane and in FP64 above that, then r <- r - fl64(V~ fl32(c)).  The recurrence, the operator products, the DGKS
 second pass, the projected solve and the certified validation stay FP64, and a
 level whose coefficients exceed 1e-3 ||r|| redoes the pass in FP64.  The
 option serves the restart cycles of the mixed form, whose corrections need a
 few digits each.
 
 * The projection itself: each coefficient must lie within
-  20 u32 ||v_j|| ||r|| of the FP64 sweep's on the same basis (two FP32
-  roundings of the inputs and a 16-term FP32 sum, with slack).
+  20 u ||v_j|| ||r|| of the FP64 sweep's on the same basis (u the copy's unit
+  roundoff, 2^-24 or 2^-11; roundings of the inputs and a 16-term FP32 sum,
+  with slack).
 * Restarted mixed solves on a ridge problem: the certified FP64 validation
   decides success, and x must agree with the restarted solve that sweeps in
   FP64 to what the energy-norm tolerance determines.  (Restart cycles suit
@@ -45,8 +46,9 @@ def _csr(prob):
                                    size=(prob.rows, prob.cols)).cuda()
 
 
+@pytest.mark.parametrize("storage", [1, 2])
 @pytest.mark.parametrize("n,k", [(5000, 37), (200_000, 64), (140_001, 96)])
-def test_reduced_projection_matches_fp64_sweep(amfls, n, k):
+def test_reduced_projection_matches_fp64_sweep(amfls, n, k, storage):
     import ctypes
     from amfls_solver_gb300 import _native
 
@@ -55,13 +57,14 @@ def test_reduced_projection_matches_fp64_sweep(amfls, n, k):
     err = ctypes.c_double(-1.0)
     stream = torch.cuda.current_stream().cuda_stream
     _native.check(lib.amfls_gpu_probe_reorthogonalization_reduced(
-        n, k, 3, ctypes.c_void_p(stream), sec, ctypes.byref(err)))
+        n, k, 3, storage, ctypes.c_void_p(stream), sec, ctypes.byref(err)))
     # the probe's basis pattern: V[row, col] = ((7 row + 13 col) mod 17 - 8) 1e-3
     rows = np.arange(n, dtype=np.int64)[:, None]
     cols = np.arange(k, dtype=np.int64)[None, :]
     v = (((rows * 7 + cols * 13) % 17) - 8) * 1e-3
     colnorm = np.sqrt((v * v).sum(axis=0)).max()
-    assert 0.0 <= err.value <= 20 * U32 * colnorm
+    u = U32 if storage == 1 else 2.0 ** -11  # the copy's unit roundoff (FP32, FP16)
+    assert 0.0 <= err.value <= 20 * u * colnorm
     assert sec[0] > 0.0 and sec[1] > 0.0
 
 
@@ -88,22 +91,23 @@ def test_restarted_ridge_solve_with_and_without_reduced_basis(amfls):
     b = torch.from_numpy(prob.b).cuda()
     reg, tol = 1e-4, 1e-10
     runs = {}
-    for rb, cycle in ((False, 1000), (True, 1000), (True, 500)):
+    for rb, cycle in ((False, 1000), (True, 1000), (True, 500), ("fp16", 1000)):
         r = amfls.run_amfls_mixed(op, b, values="fp64", reduced_basis=rb, inner_tolerance=1e-14,
                                   maximum_refinements=80, maximum_depth=cycle,
                                   regularization=reg, tolerance=tol)
         assert r.status == 0 and r.relative_energy_error_upper_bound <= tol
-        assert (r.reduced_basis_levels > 0) == rb
+        assert (r.reduced_basis_levels > 0) == bool(rb)
         assert r.reduced_basis_fallbacks <= r.reduced_basis_levels // 100
         runs[rb, cycle] = r.solution.cpu().numpy()
     norm_a = op.validation_error_model()[0]
     cond = norm_a / np.sqrt(reg)
     ref = runs[False, 1000]
-    for key in ((True, 1000), (True, 500)):
+    for key in ((True, 1000), (True, 500), ("fp16", 1000)):
         assert np.linalg.norm(runs[key] - ref) <= 4 * tol * cond * np.linalg.norm(ref)
 
 
-def test_mixed_form_against_the_reference_on_a_tall_ridge_problem(amfls):
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_mixed_form_against_the_reference_on_a_tall_ridge_problem(amfls, storage):
     """The chosen form against the reference's own solve of a 60000 x 15000
     portable CSR ridge problem (lambda = 1e-4, tol 1e-10; the reference
     certified it in 2560 levels): restart cycles of 1000 levels with
@@ -119,7 +123,7 @@ def test_mixed_form_against_the_reference_on_a_tall_ridge_problem(amfls):
     reg, tol = opts["regularization"], opts["tolerance"]
     op = amfls.DeviceOperator(_csr(prob))
     r = amfls.run_amfls_mixed(op, torch.from_numpy(prob.b).cuda(), values="fp64",
-                              reduced_basis=True, inner_tolerance=1e-14, maximum_refinements=60,
+                              reduced_basis=storage, inner_tolerance=1e-14, maximum_refinements=60,
                               maximum_depth=1000, regularization=reg, tolerance=tol)
     assert r.status == 0 and r.relative_energy_error_upper_bound <= tol
     assert r.reduced_basis_levels > 0

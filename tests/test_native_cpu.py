@@ -149,5 +149,7 @@ def test_reduced_basis_defaults_off_and_probe_checks_sizes(lib):
     o = _native.default_options()
     assert o.reduced_basis == 0 and o.use_graphs == 1
     sec = (ctypes.c_double * 2)()
-    rc = lib.amfls_gpu_probe_reorthogonalization_reduced(0, 10, 1, None, sec, None)
+    rc = lib.amfls_gpu_probe_reorthogonalization_reduced(0, 10, 1, 1, None, sec, None)
     assert rc == 1 and b"probe sizes must be positive" in lib.amfls_gpu_last_error()
+    rc = lib.amfls_gpu_probe_reorthogonalization_reduced(10, 10, 1, 3, None, sec, None)
+    assert rc == 1 and b"probe storage must be 1 (FP32) or 2 (FP16)" in lib.amfls_gpu_last_error()
