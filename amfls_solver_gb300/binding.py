@@ -120,7 +120,7 @@ class SolveResult:
     status: int
     stop_reason: int
     # GB300 extras (not in the reference's result): width-one levels whose
-    # first reorthogonalisation pass ran on the FP32 copy of the basis, and
+    # first reorthogonalisation pass ran on the reduced copy of the basis, and
     # how many of them redid it in FP64
     reduced_basis_levels: int = 0
     reduced_basis_fallbacks: int = 0

@@ -65,7 +65,7 @@ struct Statistics {
     // GB300 extras (not in the reference's tensors)
     long long projected_rank_flags = 0;
     long long kernel_launches = 0;  // kernels this solve ran on the GPU
-    long long reduced_levels = 0;     // levels projected on the FP32 copy of V
+    long long reduced_levels = 0;     // levels projected on the reduced copy of V
     long long reduced_fallbacks = 0;  // of those, levels redone in FP64
 };
 

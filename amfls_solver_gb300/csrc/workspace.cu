@@ -445,7 +445,8 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
 }
 
 // ----------------------------------------------------------------------------
-// Reduced-basis sweeps: width-one levels that keep an FP32 copy V~ of V run
+// Reduced-basis sweeps: width-one levels that keep a reduced copy V~ of V
+// (FP32, or FP16 holding 2^8 v; see RedStore) run
 // their first projection pass on it,
 //   c  = V~^T r~          r~ = fl32(r); FP32 products, FP32 sums over runs of
 //                         16 rows per lane, FP64 above that
@@ -998,7 +999,7 @@ long long sweep_part_doubles(int n, long long panels, int grid) {
     return (kSweepTargetTasksPerWarp * W + std::max(panels, tiles) + 1) * 32;
 }
 
-// v = r / ||r|| into V's new column (and the FP32 copy's, when kept) and a
+// v = r / ||r|| into V's new column (and the reduced copy's, when kept) and a
 // contiguous copy.
 template <typename S = float>
 __global__ void normalize_right_kernel(const double* r, int n, double* const* panels,
@@ -1465,7 +1466,7 @@ void Workspace::enqueue_level_kernels(cudaStream_t s, int pcap) {
     // pass, FP64 redo of a reduced pass): a few blocks per SM
     const int rare_grid = (int)std::min<long long>(tiles, 2LL * sm_count());
     if (reduced) {
-        // first pass on the FP32 copy of V; the FP64 kernels after it run
+        // first pass on the reduced copy of V; the FP64 kernels after it run
         // only when the coefficients were too large for it (sweep_fp64)
         round_residual_kernel<<<(int)std::min<long long>(grid_cap(), (n_ + 255) / 256), 256, 0,
                                 s>>>(R_, r32_, n_, dstate_);

@@ -179,7 +179,7 @@ private:
     unsigned* counter_ = nullptr;   // self-resetting tickets: misc + one per V panel
 
     std::unique_ptr<PanelStore> V_;
-    // reduced-basis sweeps: FP32 copy of V, r rounded to FP32, the FP32
+    // reduced-basis sweeps: FP32 or FP16 copy of V, r rounded to FP32, the FP32
     // coefficients, per-panel sums of c^2 and the tickets (panels | all)
     bool reduced_basis_ = false;
     int reduced_storage_ = kReducedOff;

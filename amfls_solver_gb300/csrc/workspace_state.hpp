@@ -70,7 +70,7 @@ struct DevState {
     long long search_a_calls;
     long long search_at_calls;
     long long levels_run;
-    long long reduced_levels;    // levels projected on the FP32 copy of V
+    long long reduced_levels;    // levels projected on the reduced copy of V
     long long reduced_fallbacks; // of those, levels redone in FP64
     // scalars of the current level
     double coupling;       // frontier coupling (1x1 at width one)

@@ -103,7 +103,7 @@ typedef struct {
     double timings[AMFLS_GPU_TIMINGS];
     int trace_rows; /* checkpoints evaluated; rows beyond the capacity are dropped */
     long long kernel_launches; /* GPU kernels the solve ran (not part of the reference) */
-    long long reduced_basis_levels;    /* levels projected on the FP32 copy of V (reduced_basis) */
+    long long reduced_basis_levels;    /* levels projected on the reduced copy of V (reduced_basis) */
     long long reduced_basis_fallbacks; /* of those, levels whose projection was redone in FP64 */
 } amfls_gpu_result;
 
