@@ -446,25 +446,26 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
 
 // ----------------------------------------------------------------------------
 // Reduced-basis sweeps: width-one levels that keep a reduced copy V~ of V
-// (FP32, or FP16 holding 2^8 v; see RedStore) run
-// their first projection pass on it,
+// (FP32, or FP16 holding 2^8 v; see RedStore) run their first projection
+// pass on it,
 //   c  = V~^T r~          r~ = fl32(r); FP32 products, FP32 sums over runs of
 //                         16 rows per lane, FP64 above that
 //   r <- r - fl64(V~ c~)  c~ = fl32(c); FP32 products and sums, the
 //                         subtraction in FP64
 // At width one the recurrence has already removed the previous column in
 // FP64 (the fused A^T u - beta v product), so the pass-one coefficients only
-// measure the loss of orthogonality of r against V.  Rounding V and r to
-// FP32 perturbs each coefficient by about u32 ||r|| / sqrt(n_eff) (n_eff the
-// rows the vectors spread over), which is the level of orthogonality V keeps
-// instead of FP64's; the FP32 sum V~ c~ perturbs r itself by about
-// u32 ||V c|| (at most 6e-11 ||r|| while ||c|| <= kReducedCoeffBound ||r||).
-// A level whose coefficients exceed that bound (or are not finite) redoes
-// the pass with the FP64 kernels, and the DGKS second pass is always FP64,
-// so FP64 stays on the recurrence, the correction of large components, the
-// norms and every rank decision.  The sweeps then read 4 bytes per basis
-// element on the FP32 pipe (HBM-bound) instead of 8 bytes on the FP64 pipe
-// (two FMA lanes per SM clock on this GPU).
+// measure the loss of orthogonality of r against V.  Rounding V to the copy
+// (unit roundoff u: 2^-24 FP32, 2^-11 FP16) and r to FP32 perturbs each
+// coefficient by about u ||r|| / sqrt(n_eff) (n_eff the rows the vectors
+// spread over), which is the level of orthogonality V keeps instead of
+// FP64's; the sum V~ c~ perturbs r itself by about u ||V c|| (at most
+// 5e-7 ||r|| for FP16 while ||c|| <= kReducedCoeffBound ||r||).  A level
+// whose coefficients exceed that bound (or are not finite) redoes the pass
+// with the FP64 kernels, and the DGKS second pass is always FP64, so FP64
+// stays on the recurrence, the correction of large components, the norms and
+// every rank decision.  The sweeps then read 4 or 2 bytes per basis element
+// on the FP32 pipe (HBM-bound) instead of 8 bytes on the FP64 pipe (two FMA
+// lanes per SM clock on this GPU).
 // The orthogonality this keeps suits the restart cycles of the mixed form,
 // whose corrections need a few digits each: with one-sided
 // reorthogonalisation the left basis U inherits V's orthogonality level
