@@ -449,7 +449,8 @@ v_c_kernel(double* const* __restrict__ panels, int n, int k_arg, const double* _
 // (FP32, or FP16 holding 2^8 v; see RedStore) run their first projection
 // pass on it,
 //   c  = V~^T r~          r~ = fl32(r); FP32 products, FP32 sums over runs of
-//                         16 rows per lane, FP64 above that
+//                         16 (FP32 copy) or 64 (FP16) rows per lane, FP64
+//                         above that
 //   r <- r - fl64(V~ c~)  c~ = fl32(c); FP32 products and sums, the
 //                         subtraction in FP64
 // At width one the recurrence has already removed the previous column in
@@ -479,8 +480,14 @@ constexpr double kReducedCoeffBound = 1e-3;
 // sums run in FP32 and the results are scaled back by 2^-8, exactly).
 template <typename S>
 struct RedStore;
+// kFlushSteps: steps (of 4 rows per lane) summed in FP32 before a lane's
+// partial sums go into FP64.  Each fold costs FP64 instructions (this GPU
+// retires two FP64 lanes per SM clock), which an FP16 copy, reading half the
+// bytes per element, must amortise over more rows; its own rounding (2^-11)
+// dwarfs the longer FP32 sums' (64 terms: about 2^-18).
 template <>
 struct RedStore<float> {
+    static constexpr int kFlushSteps = 4;
     static constexpr float kInvScale = 1.0f;
     __device__ static void load8(const float* p, float v[8]) {
         const float4 a = __ldcs(reinterpret_cast<const float4*>(p));
@@ -492,6 +499,7 @@ struct RedStore<float> {
 };
 template <>
 struct RedStore<__half> {
+    static constexpr int kFlushSteps = 16;
     static constexpr float kInvScale = 1.0f / 256.0f;
     __device__ static void load8(const __half* p, float v[8]) {
         const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
@@ -563,7 +571,8 @@ vt_r32_kernel(const S* const* __restrict__ panels, int n, const float* __restric
             float s8[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) s8[i] = 0.f;
-            for (int step = 0; step < 4 && base < row1; ++step, base += 256) {
+            for (int step = 0; step < RedStore<S>::kFlushSteps && base < row1;
+                 ++step, base += 256) {
                 float a[4][8];
                 float rv[4];
 #pragma unroll
@@ -690,26 +699,27 @@ v_c32_kernel(const S* const* __restrict__ panels, int n, const float* __restrict
             acc[s] = t;
         }
     }
-    double accd[4];
+    // V~ c~ is small (the pass-one coefficients are): its cross-lane and
+    // cross-warp sums stay in FP32, only the subtraction from r is FP64
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        accd[s] = (double)acc[s] * (double)RedStore<S>::kInvScale;
-        accd[s] += __shfl_xor_sync(0xffffffffu, accd[s], 1);
-        accd[s] += __shfl_xor_sync(0xffffffffu, accd[s], 2);
+        acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 1);
+        acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], 2);
     }
-    __shared__ double sm[8][32];
+    __shared__ float sm[8][32];
     __shared__ double red[32];
     if (q == 0) {
 #pragma unroll
-        for (int s = 0; s < 4; ++s) sm[warp][s * 8 + rsub] = accd[s];
+        for (int s = 0; s < 4; ++s) sm[warp][s * 8 + rsub] = acc[s];
     }
     __syncthreads();
     double sq = 0.0;
     if (threadIdx.x < 32) {
         const long long row = row0 + threadIdx.x;
-        double y = 0.0;
+        float y32 = 0.f;
 #pragma unroll
-        for (int w = 0; w < 8; ++w) y += sm[w][threadIdx.x];
+        for (int w = 0; w < 8; ++w) y32 += sm[w][threadIdx.x];
+        const double y = (double)y32 * (double)RedStore<S>::kInvScale;
         if (row < n) {
             const double o = r[row] - y;
             r[row] = o;
