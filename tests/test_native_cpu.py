@@ -153,3 +153,13 @@ def test_reduced_basis_defaults_off_and_probe_checks_sizes(lib):
     assert rc == 1 and b"probe sizes must be positive" in lib.amfls_gpu_last_error()
     rc = lib.amfls_gpu_probe_reorthogonalization_reduced(10, 10, 1, 3, None, sec, None)
     assert rc == 1 and b"probe storage must be 1 (FP32) or 2 (FP16)" in lib.amfls_gpu_last_error()
+
+
+def test_reduced_basis_argument_mapping():
+    from amfls_solver_gb300 import binding
+
+    assert [binding._reduced_storage(v) for v in (False, None, 0, True, 1, "fp32", 2, "fp16")] == \
+        [0, 0, 0, 1, 1, 1, 2, 2]
+    for bad in ("bf16", 3, 1.5):
+        with pytest.raises(ValueError):
+            binding._reduced_storage(bad)
