@@ -85,3 +85,29 @@ BASELINE_FIXTURES = sorted(p.stem for p in GOLDEN.glob("baseline_*.npz"))
 @pytest.fixture(scope="session")
 def golden():
     return load_golden
+
+
+@pytest.fixture
+def gelsy_ranks(monkeypatch):
+    """Records (shape of T, rank dgelsy found) for every projected solve the
+    oracle makes with dgelsy (krylov_workspace.cpp:833-909, lambda = 0).  The
+    GPU replaces dgelsy by a QR recurrence on T, the same least-squares
+    solution whenever dgelsy finds full column rank; the fixtures' solves must
+    all be in that case for their parity to cover the projected solve."""
+    import scipy.linalg
+    from oracle import amfls_oracle as orc
+
+    calls = []
+
+    class Recording:
+        def __getattr__(self, name):
+            return getattr(scipy.linalg, name)
+
+        def lstsq(self, a, b, **kw):
+            out = scipy.linalg.lstsq(a, b, **kw)
+            if kw.get("lapack_driver") == "gelsy":
+                calls.append((a.shape, int(out[2])))
+            return out
+
+    monkeypatch.setattr(orc, "sla", Recording())
+    return calls

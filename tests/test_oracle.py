@@ -61,7 +61,7 @@ def test_norm_interval_matches_reference():
 
 
 @pytest.mark.parametrize("name", SOLVE_FIXTURES)
-def test_oracle_solve_matches_reference(name):
+def test_oracle_solve_matches_reference(name, gelsy_ranks):
     data, prob = load_golden(name)
     opts = golden_options(data)
     if opts.pop("algorithm", "amfls") == "fixed_rbgk":
@@ -89,6 +89,9 @@ def test_oracle_solve_matches_reference(name):
             assert abs(a - b) <= rel * abs(b) + 1e-13, (idx, a, b)
         else:
             assert a == b
+    # every projected solve had full column rank in dgelsy's sense, where the
+    # GPU's QR recurrence gives the same solution
+    assert all(rank == shape[1] for shape, rank in gelsy_ranks), gelsy_ranks
 
 
 @pytest.mark.parametrize("name", CUSTOM_FIXTURES)

@@ -17,7 +17,7 @@ from oracle import amfls_oracle as orc
 
 
 @pytest.mark.parametrize("name", REPLAY_FIXTURES)
-def test_oracle_replays_reference_widening(name):
+def test_oracle_replays_reference_widening(name, gelsy_ranks):
     data, prob = load_replay(name)
     opts = golden_options(data)
     r = orc.solve_amfls(prob, replay=[int(v) for v in data["replay"]], **opts)
@@ -29,6 +29,10 @@ def test_oracle_replays_reference_widening(name):
     np.testing.assert_array_equal(r["trace_float"][:, :8], data["trace_float"][:, :8])
     xr = data["solution"]
     assert np.linalg.norm(r["solution"] - xr) <= 1e-9 * np.linalg.norm(xr)
+    # full column rank at every dgelsy projected solve (lambda = 0): the
+    # GPU's QR recurrence gives the same solution there
+    assert all(rank == shape[1] for shape, rank in gelsy_ranks), gelsy_ranks
+    assert gelsy_ranks or opts["regularization"] > 0.0
 
 
 def test_replay_fixtures_widen():
