@@ -196,6 +196,17 @@ def replays():
                    regularization=1e-4, tolerance=1e-10)
 
 
+def full_size():
+    """The 100000 x 2000 dense ridge configuration at full size, on the
+    portable generator (the same bytes on every platform; condition about
+    2^20, a uniform right-hand side, lambda = 1e-6, tol 1e-10).  The
+    reference needs about two minutes per run for it, so it has its own
+    argument."""
+    replay_fixture("replay_dense_ridge_100000x2000",
+                   ("portable_dense", dict(m=100000, n=2000, octaves=20, seed=20251203)),
+                   regularization=1e-6, tolerance=1e-10)
+
+
 def main():
     # ---- kernels: CSR products, validation model, Gaussian, norm intervals
     p = problems.scaled_uniform_csr(300, 120, per_row=7, decades=3.0, seed=11)
@@ -315,9 +326,11 @@ def baselines():
 if __name__ == "__main__":
     # no argument: every fixture; "baselines": only the LSQR / LSMR ones;
     # "replays": only the schedule-replay fixtures; "customs": only the
-    # custom-operator ones
+    # custom-operator ones; "full": only the full-size dense ridge solve
     if sys.argv[1:] == ["baselines"]:
         baselines()
+    elif sys.argv[1:] == ["full"]:
+        full_size()
     elif sys.argv[1:] == ["replays"]:
         replays()
     elif sys.argv[1:] == ["customs"]:
@@ -327,3 +340,4 @@ if __name__ == "__main__":
         baselines()
         replays()
         customs()
+        full_size()
