@@ -79,6 +79,8 @@ amfls_gpu::SolveOptions to_options(const amfls_gpu_options* o) {
     s.stop_early = o->stop_early != 0;
     s.time_operators = o->time_operators != 0;
     s.use_graphs = o->use_graphs != 0;
+    if (o->reduced_basis < 0 || o->reduced_basis > 2)
+        throw std::invalid_argument("options.reduced_basis must be 0 (off), 1 (FP32) or 2 (FP16)");
     s.reduced_basis = o->reduced_basis;
     return s;
 }
@@ -248,9 +250,9 @@ int amfls_gpu_solve_amfls(const amfls_gpu_operator* op, const double* d_b,
                           amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
                           int trace_capacity, void* stream) {
     return guarded([&] {
+        const auto opts = to_options(options);  // option errors before any device work
         if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
-        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, to_options(options), d_solution,
-                                              as_stream(stream));
+        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, opts, d_solution, as_stream(stream));
         export_result(r, result, trace_float, trace_int, trace_capacity);
     });
 }
@@ -260,9 +262,10 @@ int amfls_gpu_solve_fixed_rbgk(const amfls_gpu_operator* op, const double* d_b,
                                amfls_gpu_result* result, double* trace_float, int64_t* trace_int,
                                int trace_capacity, void* stream) {
     return guarded([&] {
+        const auto opts = to_options(options);
         if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
-        const auto r = amfls_gpu::solve_fixed_rbgk(deref(op), d_b, to_options(options),
-                                                   d_solution, as_stream(stream));
+        const auto r = amfls_gpu::solve_fixed_rbgk(deref(op), d_b, opts, d_solution,
+                                                   as_stream(stream));
         export_result(r, result, trace_float, trace_int, trace_capacity);
     });
 }
@@ -329,8 +332,9 @@ int amfls_gpu_solve_amfls_mixed(const amfls_gpu_operator* op, const amfls_gpu_op
                                 double* trace_float, int64_t* trace_int, int trace_capacity,
                                 void* stream) {
     return guarded([&] {
-        const auto r = amfls_gpu::solve_amfls_mixed(deref(op), deref(reduced), d_b,
-                                                    to_options(options), inner_tolerance,
+        const auto opts = to_options(options);
+        const auto r = amfls_gpu::solve_amfls_mixed(deref(op), deref(reduced), d_b, opts,
+                                                    inner_tolerance,
                                                     maximum_refinements, d_solution,
                                                     as_stream(stream));
         export_result(r, result, trace_float, trace_int, trace_capacity);
@@ -432,7 +436,8 @@ int amfls_gpu_solve_amfls_controlled(const amfls_gpu_operator* op, const double*
         ctl.exploration = exploration;
         ctl.exploration_seed = exploration_seed;
         ctl.log = &log;
-        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, to_options(options), d_solution,
+        const auto opts = to_options(options);
+        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, opts, d_solution,
                                               as_stream(stream), &ctl);
         export_result(r, result, trace_float, trace_int, trace_capacity);
         const int rows = std::min<int>(decision_capacity, (int)log.size());
@@ -456,6 +461,7 @@ int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b
                                  double* trace_float, int64_t* trace_int, int trace_capacity,
                                  void* stream) {
     return guarded([&] {
+        const auto opts = to_options(options);
         if (d_solution == nullptr) throw std::invalid_argument("solution must not be null");
         if (replay_count > 0 && replay == nullptr)
             throw std::invalid_argument("replay list must not be null");
@@ -468,7 +474,7 @@ int amfls_gpu_solve_amfls_replay(const amfls_gpu_operator* op, const double* d_b
         ctl.replay_count = replay_count < 0 ? -1 : replay_count;
         ctl.sites = &sites;
         ctl.overrun = &overrun;
-        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, to_options(options), d_solution,
+        const auto r = amfls_gpu::solve_amfls(deref(op), d_b, opts, d_solution,
                                               as_stream(stream), &ctl);
         export_result(r, result, trace_float, trace_int, trace_capacity);
         const int n = std::min<int>(decision_capacity, (int)sites.size());
@@ -518,9 +524,9 @@ int amfls_gpu_solve_amfls_batch(int count, const amfls_gpu_operator* const* ops,
             throw std::invalid_argument("batch arrays must not be null");
         std::vector<amfls_gpu::BatchItem> items(count);
         for (int i = 0; i < count; ++i) {
+            items[i].options = to_options(&options[i]);
             items[i].op = &deref(ops[i]);
             items[i].b = d_b[i];
-            items[i].options = to_options(&options[i]);
             items[i].x = d_solutions[i];
         }
         const auto out = amfls_gpu::solve_amfls_batch(items, workers, wall_seconds);

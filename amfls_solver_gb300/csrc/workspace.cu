@@ -1249,67 +1249,76 @@ Workspace::Workspace(const DeviceOperator& op, const double* d_b, double regular
     if (!std::isfinite(regularization) || regularization < 0.0)
         throw std::invalid_argument("block Golub-Kahan regularization must be finite and nonnegative");
     if (maximum_basis_size < 0) throw std::invalid_argument("block Golub-Kahan basis limit must be nonnegative");
-    keep_pool_memory();
-    const int mn = std::min(m_, n_);
-    basis_limit_ = maximum_basis_size > 0 ? std::min(maximum_basis_size, mn) : mn;
-    stream_alloc(&dstate_, sizeof(DevState), stream_);
-    stream_alloc(&red_, sizeof(RedResult) * 4, stream_);
-    // scratch: V^T r partials ((target blocks + panels) x 32), then the
-    // per-block norm partials of the V c sweep (n/32 + slack)
-    const long long max_panels = basis_limit_ / 32 + 2;
-    vc_partials_offset_ = (kMaxGemvTargetBlocks + max_panels) * 32 + 6 * kMaxGridCap;
-    const long long pcount = vc_partials_offset_ + (n_ + 31) / 32 + 1024;
-    stream_alloc(&partials_, sizeof(double) * pcount, stream_);
-    sweep_grid_ = sweep_grid();
-    warp_sweeps_ = use_warp_sweeps(n_);
-    sweep_panels_ = max_panels;
-    const long long tiles = (n_ + 31) / 32;
-    stream_alloc(&sweep_part_, sizeof(double) * sweep_part_doubles(n_, max_panels, sweep_grid_),
-                 stream_);
-    stream_alloc(&sweep_sq_, sizeof(double) * tiles, stream_);
-    stream_alloc(&sweep_tickets_, sizeof(unsigned) * (max_panels + tiles + 1), stream_);
-    AMFLS_CUDA(cudaMemsetAsync(sweep_tickets_, 0, sizeof(unsigned) * (max_panels + tiles + 1),
-                               stream_));
-    const long long ncounters = 64 + max_panels + 64;
-    stream_alloc(&counter_, sizeof(unsigned) * ncounters, stream_);
-    AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * ncounters, stream_));
-    stream_alloc(&R_, sizeof(double) * n_, stream_);
-    stream_alloc(&vnew_, sizeof(double) * n_, stream_);
-    stream_alloc(&Y_, sizeof(double) * m_, stream_);
-    ucap_ = 1;
-    stream_alloc(&U_, sizeof(double) * m_ * ucap_, stream_);
-    V_ = std::make_unique<PanelStore>(n_, static_cast<int>(max_panels), stream_);
-    V_->ensure_columns(1);  // panel 0 exists (zeroed) before any level runs
     if (reduced_basis != kReducedOff && reduced_basis != kReducedFp32 &&
         reduced_basis != kReducedFp16)
         throw std::invalid_argument("reduced_basis must be 0 (off), 1 (FP32) or 2 (FP16)");
-    reduced_storage_ = reduced_basis;
-    reduced_basis_ = reduced_basis != kReducedOff;
-    if (reduced_basis_) {
-        if (reduced_storage_ == kReducedFp16) {
-            V16_ = std::make_unique<PanelStore16>(n_, static_cast<int>(max_panels), stream_);
-            V16_->ensure_columns(1);
-        } else {
-            V32_ = std::make_unique<PanelStore32>(n_, static_cast<int>(max_panels), stream_);
-            V32_->ensure_columns(1);
-        }
-        red_grid_ = reduced_sweep_grid();
-        stream_alloc(&r32_, sizeof(float) * n_, stream_);
-        stream_alloc(&panel_sq_, sizeof(double) * max_panels, stream_);
-        stream_alloc(&red_part_, sizeof(double) * reduced_part_doubles(red_grid_, max_panels),
+    keep_pool_memory();
+    try {
+        const int mn = std::min(m_, n_);
+        basis_limit_ = maximum_basis_size > 0 ? std::min(maximum_basis_size, mn) : mn;
+        stream_alloc(&dstate_, sizeof(DevState), stream_);
+        stream_alloc(&red_, sizeof(RedResult) * 4, stream_);
+        // scratch: V^T r partials ((target blocks + panels) x 32), then the
+        // per-block norm partials of the V c sweep (n/32 + slack)
+        const long long max_panels = basis_limit_ / 32 + 2;
+        vc_partials_offset_ = (kMaxGemvTargetBlocks + max_panels) * 32 + 6 * kMaxGridCap;
+        const long long pcount = vc_partials_offset_ + (n_ + 31) / 32 + 1024;
+        stream_alloc(&partials_, sizeof(double) * pcount, stream_);
+        sweep_grid_ = sweep_grid();
+        warp_sweeps_ = use_warp_sweeps(n_);
+        sweep_panels_ = max_panels;
+        const long long tiles = (n_ + 31) / 32;
+        stream_alloc(&sweep_part_, sizeof(double) * sweep_part_doubles(n_, max_panels, sweep_grid_),
                      stream_);
-        stream_alloc(&red_tickets_, sizeof(unsigned) * (max_panels + 1), stream_);
-        AMFLS_CUDA(cudaMemsetAsync(red_tickets_, 0, sizeof(unsigned) * (max_panels + 1), stream_));
+        stream_alloc(&sweep_sq_, sizeof(double) * tiles, stream_);
+        stream_alloc(&sweep_tickets_, sizeof(unsigned) * (max_panels + tiles + 1), stream_);
+        AMFLS_CUDA(cudaMemsetAsync(sweep_tickets_, 0, sizeof(unsigned) * (max_panels + tiles + 1),
+                                   stream_));
+        const long long ncounters = 64 + max_panels + 64;
+        stream_alloc(&counter_, sizeof(unsigned) * ncounters, stream_);
+        AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * ncounters, stream_));
+        stream_alloc(&R_, sizeof(double) * n_, stream_);
+        stream_alloc(&vnew_, sizeof(double) * n_, stream_);
+        stream_alloc(&Y_, sizeof(double) * m_, stream_);
+        ucap_ = 1;
+        stream_alloc(&U_, sizeof(double) * m_ * ucap_, stream_);
+        V_ = std::make_unique<PanelStore>(n_, static_cast<int>(max_panels), stream_);
+        V_->ensure_columns(1);  // panel 0 exists (zeroed) before any level runs
+        reduced_storage_ = reduced_basis;
+        reduced_basis_ = reduced_basis != kReducedOff;
+        if (reduced_basis_) {
+            if (reduced_storage_ == kReducedFp16) {
+                V16_ = std::make_unique<PanelStore16>(n_, static_cast<int>(max_panels), stream_);
+                V16_->ensure_columns(1);
+            } else {
+                V32_ = std::make_unique<PanelStore32>(n_, static_cast<int>(max_panels), stream_);
+                V32_->ensure_columns(1);
+            }
+            red_grid_ = reduced_sweep_grid();
+            stream_alloc(&r32_, sizeof(float) * n_, stream_);
+            stream_alloc(&panel_sq_, sizeof(double) * max_panels, stream_);
+            stream_alloc(&red_part_, sizeof(double) * reduced_part_doubles(red_grid_, max_panels),
+                         stream_);
+            stream_alloc(&red_tickets_, sizeof(unsigned) * (max_panels + 1), stream_);
+            AMFLS_CUDA(cudaMemsetAsync(red_tickets_, 0, sizeof(unsigned) * (max_panels + 1),
+                                       stream_));
+        }
+        AMFLS_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
+        std::memset(&host_, 0, sizeof(host_));
+        host_.reliable = 1;
+        host_.basis_limit = basis_limit_;
+        AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice,
+                                   stream_));
+        stream_wait(stream_);
+    } catch (...) {  // e.g. out of device memory part way: free what was allocated
+        release();
+        throw;
     }
-    AMFLS_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
-    std::memset(&host_, 0, sizeof(host_));
-    host_.reliable = 1;
-    host_.basis_limit = basis_limit_;
-    AMFLS_CUDA(cudaMemcpyAsync(dstate_, &host_, sizeof(DevState), cudaMemcpyHostToDevice, stream_));
-    stream_wait(stream_);
 }
 
-Workspace::~Workspace() {
+Workspace::~Workspace() { release(); }
+
+void Workspace::release() noexcept {
     cudaStreamSynchronize(stream_);
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
     if (graph_) cudaGraphDestroy(graph_);

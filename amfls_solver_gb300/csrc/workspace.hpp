@@ -116,6 +116,9 @@ public:
     bool reduced_basis() const { return reduced_basis_; }
 
 private:
+    // frees every device buffer, stream, graph and event the workspace holds
+    // (the destructor, and a constructor that fails after allocating)
+    void release() noexcept;
     void enqueue_level_kernels(cudaStream_t s, int pcap);
     void build_graph(int pcap);
     void invalidate_graph();

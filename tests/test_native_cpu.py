@@ -155,6 +155,43 @@ def test_reduced_basis_defaults_off_and_probe_checks_sizes(lib):
     assert rc == 1 and b"probe storage must be 1 (FP32) or 2 (FP16)" in lib.amfls_gpu_last_error()
 
 
+def test_invalid_reduced_basis_is_rejected_before_device_work(lib):
+    """Every solve entry point converts its options first: an out-of-range
+    reduced_basis is an argument error, reported before the operator is
+    looked at or anything is allocated."""
+    o = _native.default_options()
+    o.reduced_basis = 3
+    res = _native.Result()
+    dummy = ctypes.c_void_p(16)
+    expect = b"options.reduced_basis must be 0 (off), 1 (FP32) or 2 (FP16)"
+    calls = {
+        "solve_amfls": lambda: lib.amfls_gpu_solve_amfls(
+            None, None, ctypes.byref(o), dummy, ctypes.byref(res), None, None, 0, None),
+        "solve_fixed_rbgk": lambda: lib.amfls_gpu_solve_fixed_rbgk(
+            None, None, ctypes.byref(o), dummy, ctypes.byref(res), None, None, 0, None),
+        "solve_amfls_mixed": lambda: lib.amfls_gpu_solve_amfls_mixed(
+            None, None, None, ctypes.byref(o), 1e-6, 4, dummy, ctypes.byref(res), None, None, 0,
+            None),
+        "solve_amfls_controlled": lambda: lib.amfls_gpu_solve_amfls_controlled(
+            None, None, ctypes.byref(o), None, 0.0, 0, None, 0, None, dummy, ctypes.byref(res),
+            None, None, 0, None),
+        "solve_amfls_replay": lambda: lib.amfls_gpu_solve_amfls_replay(
+            None, None, ctypes.byref(o), None, 0, None, 0, None, None, dummy,
+            ctypes.byref(res), None, None, 0, None),
+    }
+    for name, call in calls.items():
+        assert call() == 1, name
+        assert expect in lib.amfls_gpu_last_error(), name
+    ops = (ctypes.c_void_p * 1)(None)
+    bs = (ctypes.c_void_p * 1)(16)
+    xs = (ctypes.c_void_p * 1)(16)
+    rc = lib.amfls_gpu_solve_amfls_batch(1, ops, bs, ctypes.byref(o), xs, ctypes.byref(res),
+                                         None, 1, None)
+    assert rc == 1 and expect in lib.amfls_gpu_last_error()
+    o.reduced_basis = -1
+    assert calls["solve_amfls"]() == 1 and expect in lib.amfls_gpu_last_error()
+
+
 def test_reduced_basis_argument_mapping():
     from amfls_solver_gb300 import binding
 
