@@ -91,7 +91,9 @@ typedef struct {
                                     an ill-conditioned problem to FP64 accuracy can stall on
                                     it (reported by the certificate, never a false success).
                                     Costs 4 (FP32) or 2 (FP16) extra bytes per basis element
-                                    of device memory. */
+                                    of device memory.  Any other value makes every solve
+                                    entry point return AMFLS_GPU_INVALID_ARGUMENT before any
+                                    device work. */
 } amfls_gpu_options;
 
 /* LeastSquaresResult, packed like the torch binding's tensors. */
