@@ -317,45 +317,58 @@ DenseOperator::DenseOperator(int rows, int cols, const double* d_values, bool co
         throw std::invalid_argument("dense operator input is invalid");
     const int outer = column_major ? cols : rows;
     const int inner = column_major ? rows : cols;
-    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kMaxGridCap + 64)));
-    AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * 8));
-    AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * 8, stream));
-    AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows, cols)));
-    // partial sums of the chunked products, sized once so that products can
-    // be captured into CUDA graphs
-    for (int tr = 0; tr < 2; ++tr) {  // both directions, up to 8 columns per pass
-        const int on = tr ? cols : rows, inn = tr ? rows : cols;
-        int bx = 0, ch = 0, ck = 0;
-        block_chunks(column_major == (tr == 1), on, inn, bx, ch, ck);
-        partial_cap_ = std::max(partial_cap_, 8LL * ch * on);
+    double* w = nullptr;  // model workspace, freed before returning
+    double model[2] = {0.0, 0.0};
+    try {
+        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * (6 * kMaxGridCap + 64)));
+        AMFLS_CUDA(cudaMalloc(&counter_, sizeof(unsigned) * 8));
+        AMFLS_CUDA(cudaMemsetAsync(counter_, 0, sizeof(unsigned) * 8, stream));
+        AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * std::max(rows, cols)));
+        // partial sums of the chunked products, sized once so that products
+        // can be captured into CUDA graphs
+        for (int tr = 0; tr < 2; ++tr) {  // both directions, up to 8 columns per pass
+            const int on = tr ? cols : rows, inn = tr ? rows : cols;
+            int bx = 0, ch = 0, ck = 0;
+            block_chunks(column_major == (tr == 1), on, inn, bx, ch, ck);
+            partial_cap_ = std::max(partial_cap_, 8LL * ch * on);
+        }
+        AMFLS_CUDA(cudaMalloc(&partials_,
+                              sizeof(double) * std::max<long long>(1, partial_cap_)));
+        // w: acc[5] | frob(inner) | model[2] | frob(outer) | partials (inner) | partials (outer)
+        const int ig = grid_1d(inner), og = grid_1d(outer);
+        AMFLS_CUDA(cudaMallocAsync(&w, sizeof(double) * (9 + ig + og), stream));
+        AMFLS_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * (9 + ig + og), stream));
+        model_outer_kernel<<<og, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9 + ig,
+                                                        counter_ + 2, w + 8);
+        AMFLS_LAUNCHED();
+        model_inner_kernel<<<ig, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9, counter_,
+                                                        w + 5);
+        AMFLS_LAUNCHED();
+        // the reference's Frobenius bound sums column square sums: the inner
+        // index for row-major storage, the outer one for column-major
+        model_finish_kernel<<<1, 1, 0, stream>>>(w, column_major ? w + 8 : w + 5,
+                                                 column_major ? 0 : 1, w + 6);
+        AMFLS_LAUNCHED();
+        AMFLS_CUDA(cudaMemcpyAsync(model, w + 6, sizeof(model), cudaMemcpyDeviceToHost,
+                                   stream));
+        AMFLS_CUDA(cudaStreamSynchronize(stream));
+        double* used = w;
+        w = nullptr;
+        AMFLS_CUDA(cudaFreeAsync(used, stream));
+    } catch (...) {  // e.g. out of device memory part way: free what was allocated
+        if (w) cudaFreeAsync(w, stream);
+        release();
+        throw;
     }
-    AMFLS_CUDA(cudaMalloc(&partials_, sizeof(double) * std::max<long long>(1, partial_cap_)));
-    // w: acc[5] | frob(inner) | model[2] | frob(outer) | partials (inner) | partials (outer)
-    double* w = nullptr;
-    const int ig = grid_1d(inner), og = grid_1d(outer);
-    AMFLS_CUDA(cudaMallocAsync(&w, sizeof(double) * (9 + ig + og), stream));
-    AMFLS_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * (9 + ig + og), stream));
-    model_outer_kernel<<<og, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9 + ig, counter_ + 2,
-                                                    w + 8);
-    AMFLS_LAUNCHED();
-    model_inner_kernel<<<ig, kThreads, 0, stream>>>(a_, outer, inner, w, w + 9, counter_, w + 5);
-    AMFLS_LAUNCHED();
-    // the reference's Frobenius bound sums column square sums: the inner
-    // index for row-major storage, the outer one for column-major
-    model_finish_kernel<<<1, 1, 0, stream>>>(w, column_major ? w + 8 : w + 5,
-                                             column_major ? 0 : 1, w + 6);
-    AMFLS_LAUNCHED();
-    double model[2];
-    AMFLS_CUDA(cudaMemcpyAsync(model, w + 6, sizeof(model), cudaMemcpyDeviceToHost, stream));
-    AMFLS_CUDA(cudaStreamSynchronize(stream));
-    AMFLS_CUDA(cudaFreeAsync(w, stream));
     model_.norm_upper = model[0];
     model_.norm_lower = model[1];
     model_.apply_steps = 2LL * cols + 2LL;
     model_.transpose_steps = 2LL * rows + 2LL;
 }
 
-DenseOperator::~DenseOperator() {
+DenseOperator::~DenseOperator() { release(); }
+
+void DenseOperator::release() noexcept {
     cudaFree(partials_);
     cudaFree(tmp_);
     cudaFree(scratch_);

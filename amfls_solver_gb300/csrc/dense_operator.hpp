@@ -37,6 +37,7 @@ public:
                   cudaStream_t s) const override;
 
 private:
+    void release() noexcept;  // frees the operator's device buffers
     void product(bool transpose, const double* x, double* y, const int* guard,
                  cudaStream_t s) const;
     void block_product(bool transpose, const double* x, int block_cols, double* y,
