@@ -30,12 +30,18 @@ CallbackOperator::CallbackOperator(int rows, int cols, const Callbacks& cb, cuda
             m.transpose_steps < 0)
             throw std::invalid_argument("custom operator validation model is invalid");
     }
-    AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * (size_t)std::max(rows, cols)));
-    AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxGridCap + 64));
-    counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
-                                           sizeof(double) * 6 * kMaxGridCap);
-    AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
-    AMFLS_CUDA(cudaStreamSynchronize(stream));
+    try {
+        AMFLS_CUDA(cudaMalloc(&tmp_, sizeof(double) * (size_t)std::max(rows, cols)));
+        AMFLS_CUDA(cudaMalloc(&scratch_, sizeof(double) * 6 * kMaxGridCap + 64));
+        counter_ = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(scratch_) +
+                                               sizeof(double) * 6 * kMaxGridCap);
+        AMFLS_CUDA(cudaMemsetAsync(counter_, 0, 64, stream));
+        AMFLS_CUDA(cudaStreamSynchronize(stream));
+    } catch (...) {  // free what was allocated before the failure
+        cudaFree(tmp_);
+        cudaFree(scratch_);
+        throw;
+    }
 }
 
 CallbackOperator::~CallbackOperator() {

@@ -134,14 +134,14 @@ SolveResult solve_amfls_mixed(const DeviceOperator& op, const DeviceOperator& re
     const long long ma = ridge ? m + n : m;  // rows of M
 
     double *res = nullptr, *dx = nullptr;
+    struct Free {  // frees both buffers however the solve ends
+        double** p[2];
+        ~Free() {
+            for (double** q : p) cudaFree(*q);
+        }
+    } release{{&res, &dx}};
     AMFLS_CUDA(cudaMalloc(&res, sizeof(double) * ma));
     AMFLS_CUDA(cudaMalloc(&dx, sizeof(double) * n));
-    struct Free {
-        double* p[2];
-        ~Free() {
-            for (double* q : p) cudaFree(q);
-        }
-    } release{{res, dx}};
 
     // inner operators: M~ on the reduced operator, and M on the FP64 one
     // for the steps after the reduced ones stop contracting

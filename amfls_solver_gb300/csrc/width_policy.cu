@@ -140,28 +140,35 @@ struct Buffers {
         if ((int)params.size() != kPolicyParams)
             throw std::invalid_argument("policy parameter vector has the wrong length");
         const size_t nn = n;
-        AMFLS_CUDA(cudaMalloc(&x, sizeof(double) * nn * I));
-        AMFLS_CUDA(cudaMalloc(&y, sizeof(double) * nn));
-        AMFLS_CUDA(cudaMalloc(&h1, sizeof(double) * nn * H));
-        AMFLS_CUDA(cudaMalloc(&h2, sizeof(double) * nn * H));
-        AMFLS_CUDA(cudaMalloc(&out, sizeof(double) * nn));
-        AMFLS_CUDA(cudaMalloc(&d1, sizeof(double) * nn * H));
-        AMFLS_CUDA(cudaMalloc(&d2, sizeof(double) * nn * H));
-        AMFLS_CUDA(cudaMalloc(&d3, sizeof(double) * nn));
-        AMFLS_CUDA(cudaMalloc(&sq, sizeof(double) * nn));
-        AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * kPolicyParams));
-        AMFLS_CUDA(cudaMalloc(&g, sizeof(double) * kPolicyParams));
-        AMFLS_CUDA(cudaMalloc(&m, sizeof(double) * kPolicyParams));
-        AMFLS_CUDA(cudaMalloc(&v, sizeof(double) * kPolicyParams));
-        AMFLS_CUDA(cudaMalloc(&loss, sizeof(double)));
-        AMFLS_CUDA(cudaMemcpyAsync(x, hx, sizeof(double) * nn * I, cudaMemcpyHostToDevice, s));
-        if (hy) AMFLS_CUDA(cudaMemcpyAsync(y, hy, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
-        AMFLS_CUDA(cudaMemcpyAsync(p, params.data(), sizeof(double) * kPolicyParams,
-                                   cudaMemcpyHostToDevice, s));
-        AMFLS_CUDA(cudaMemsetAsync(m, 0, sizeof(double) * kPolicyParams, s));
-        AMFLS_CUDA(cudaMemsetAsync(v, 0, sizeof(double) * kPolicyParams, s));
+        try {
+            AMFLS_CUDA(cudaMalloc(&x, sizeof(double) * nn * I));
+            AMFLS_CUDA(cudaMalloc(&y, sizeof(double) * nn));
+            AMFLS_CUDA(cudaMalloc(&h1, sizeof(double) * nn * H));
+            AMFLS_CUDA(cudaMalloc(&h2, sizeof(double) * nn * H));
+            AMFLS_CUDA(cudaMalloc(&out, sizeof(double) * nn));
+            AMFLS_CUDA(cudaMalloc(&d1, sizeof(double) * nn * H));
+            AMFLS_CUDA(cudaMalloc(&d2, sizeof(double) * nn * H));
+            AMFLS_CUDA(cudaMalloc(&d3, sizeof(double) * nn));
+            AMFLS_CUDA(cudaMalloc(&sq, sizeof(double) * nn));
+            AMFLS_CUDA(cudaMalloc(&p, sizeof(double) * kPolicyParams));
+            AMFLS_CUDA(cudaMalloc(&g, sizeof(double) * kPolicyParams));
+            AMFLS_CUDA(cudaMalloc(&m, sizeof(double) * kPolicyParams));
+            AMFLS_CUDA(cudaMalloc(&v, sizeof(double) * kPolicyParams));
+            AMFLS_CUDA(cudaMalloc(&loss, sizeof(double)));
+            AMFLS_CUDA(cudaMemcpyAsync(x, hx, sizeof(double) * nn * I, cudaMemcpyHostToDevice, s));
+            if (hy)
+                AMFLS_CUDA(cudaMemcpyAsync(y, hy, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+            AMFLS_CUDA(cudaMemcpyAsync(p, params.data(), sizeof(double) * kPolicyParams,
+                                       cudaMemcpyHostToDevice, s));
+            AMFLS_CUDA(cudaMemsetAsync(m, 0, sizeof(double) * kPolicyParams, s));
+            AMFLS_CUDA(cudaMemsetAsync(v, 0, sizeof(double) * kPolicyParams, s));
+        } catch (...) {  // free what was allocated before the failure
+            free_all();
+            throw;
+        }
     }
-    ~Buffers() {
+    ~Buffers() { free_all(); }
+    void free_all() noexcept {
         for (double* q : {x, y, h1, h2, out, d1, d2, d3, sq, p, g, m, v, loss}) cudaFree(q);
     }
     // forward + backward: gradient in g, loss in *loss
@@ -212,10 +219,16 @@ WidthPolicy::WidthPolicy(const std::vector<double>& params) {
         throw std::invalid_argument("policy parameter vector has the wrong length");
     for (double v : params)
         if (!std::isfinite(v)) throw std::invalid_argument("policy parameters must be finite");
-    AMFLS_CUDA(cudaMalloc(&params_, sizeof(double) * kPolicyParams));
-    AMFLS_CUDA(cudaMalloc(&io_, sizeof(double) * (2 * I + 2)));
-    AMFLS_CUDA(cudaMemcpy(params_, params.data(), sizeof(double) * kPolicyParams,
-                          cudaMemcpyHostToDevice));
+    try {
+        AMFLS_CUDA(cudaMalloc(&params_, sizeof(double) * kPolicyParams));
+        AMFLS_CUDA(cudaMalloc(&io_, sizeof(double) * (2 * I + 2)));
+        AMFLS_CUDA(cudaMemcpy(params_, params.data(), sizeof(double) * kPolicyParams,
+                              cudaMemcpyHostToDevice));
+    } catch (...) {  // free what was allocated before the failure
+        cudaFree(params_);
+        cudaFree(io_);
+        throw;
+    }
 }
 
 WidthPolicy::~WidthPolicy() {
