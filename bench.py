@@ -365,8 +365,9 @@ def c3_measurement(dev):
         del plain
         torch.cuda.empty_cache()
         # the chosen form: FP64 residual correction around restart cycles of
-        # C3_CYCLE levels whose first reorthogonalisation pass runs on an FP32
-        # copy of the basis (products, recurrence and validation in FP64)
+        # C3_CYCLE levels whose first reorthogonalisation pass runs on a
+        # C3_STORAGE copy of the basis (products, recurrence and validation
+        # in FP64)
         mixed, t_mixed = timed_solve(lambda: amfls.run_amfls_mixed(
             op, b, values="fp64", reduced_basis=C3_STORAGE, inner_tolerance=1e-14,
             maximum_refinements=40, maximum_depth=C3_CYCLE, **opts))
