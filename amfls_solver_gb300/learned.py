@@ -50,7 +50,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .binding import TRACE_CAPACITY, DeviceOperator, SolveResult, _decode, _stream_handle, _uint64
+from .binding import TRACE_CAPACITY, DeviceOperator, _decode, _stream_handle, _uint64
 
 F = _native.POLICY_FEATURES
 IN = _native.POLICY_INPUTS
