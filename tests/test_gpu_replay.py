@@ -1,5 +1,6 @@
 """The CUDA solve in schedule-replay mode against the reference's widening
-solves and the 20000 x 5000 CSR workload.
+solves, the 20000 x 5000 CSR workload and the full-size 100000 x 2000 dense
+ridge problem.
 
 The reference's width controller weighs measured seconds, so on its own the
 GPU takes other widening decisions than the CPU reference.  Replaying the
